@@ -1,0 +1,164 @@
+/*
+ * lqmc_gpu.h -- C ABI of liblqmc_gpu.so, the GB300 (sm_103a) engine for the DQMC sweep
+ * hot path of KieDani/LatticeQMC (package `lqmc`).
+ *
+ * The reference is pure Python; its "interface" for this path is the LatticeQMC solver
+ * (lqmc/lqmc.py).  Each entry point below replaces one piece of it; the Python facade in
+ * latticeqmc_gb300/ binds these symbols with ctypes and keeps the reference's API
+ * (HubbardModel / Configuration / LatticeQMC / measure / measure_betas).
+ *
+ * Conventions
+ *   - Every function returns 0 (LQMC_OK) or a negative LQMC_ERR_* code; no exception or
+ *     abort crosses the ABI.  lqmc_last_error() gives a message for the last failure.
+ *   - Plain pointers and sizes only.  Matrices are float64, row-major (C order), n x n.
+ *     The Hubbard-Stratonovich field crosses the ABI in the reference's (n_sites,
+ *     time_steps) int8 layout (lqmc/configuration.py:89) and is held on the device as
+ *     [slice][site] so that one time slice is contiguous.
+ *   - Host buffers in, host buffers out: the handle owns every device buffer it uses
+ *     (allocated in lqmc_set_chains, freed in lqmc_destroy).
+ *   - lqmc_sweep is asynchronous on the given stream (NULL = the default stream);
+ *     lqmc_get_* synchronise that stream.
+ *   - A handle is not thread-safe: use one host thread per handle.
+ *   - Algorithm mode, precision and RNG are fixed at lqmc_create.
+ */
+#ifndef LQMC_GPU_H
+#define LQMC_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LQMC_ABI_VERSION 1
+
+/* return codes */
+#define LQMC_OK 0
+#define LQMC_ERR_INVALID -1      /* bad argument (size, index, null pointer, ...)      */
+#define LQMC_ERR_CUDA -2         /* a CUDA runtime call failed                          */
+#define LQMC_ERR_STATE -3        /* call out of order (e.g. sweep before set_chains)   */
+#define LQMC_ERR_UNSUPPORTED -4  /* combination not built (e.g. compat + mixed)         */
+#define LQMC_ERR_NUMERIC -5      /* a chain reported non-finite G or a zero pivot       */
+#define LQMC_ERR_NOMEM -6        /* device allocation failed                            */
+
+/* algorithm modes */
+#define LQMC_MODE_COMPAT 0   /* replays lqmc.py:301-347 arithmetic, defects included     */
+#define LQMC_MODE_DQMC 1     /* textbook DQMC, QR/UDV stabilised                          */
+
+/* precisions */
+#define LQMC_PREC_FP64 0     /* every floating-point operation in float64                */
+#define LQMC_PREC_MIXED 1    /* float32 G, wraps and delayed updates; FP64 stabilisation */
+
+/* uniform-draw sources */
+#define LQMC_RNG_REPLAY 0    /* caller uploads the uniforms (e.g. numpy's stream)        */
+#define LQMC_RNG_PHILOX 1    /* Philox4x64-10 on the device, keyed by (seed, chain)      */
+
+/* per-chain status bits (lqmc_get_status) */
+#define LQMC_STATUS_NONFINITE 1   /* NaN/Inf found in G                                  */
+#define LQMC_STATUS_SINGULAR 2    /* zero pivot in an LU factorisation                   */
+#define LQMC_STATUS_DRIFT 4       /* stabilisation residual above the drift threshold    */
+
+/* observable vector layout returned by lqmc_get_observables (per chain), float64:
+ *   [0] number of measurements       [1] sum of kinetic energy   [2] sum of potential energy
+ *   [3] sum of mean double occupancy [4] sum of mean density     [5..7] reserved
+ *   [8 .. 8+N)        per-site density sums
+ *   [8+N .. 8+2N)     per-site double-occupancy sums
+ *   [8+2N .. 8+2N+N^2)        <n_i n_j> sums
+ *   [8+2N+N^2 .. 8+2N+2N^2)   <S^z_i S^z_j> sums                                         */
+#define LQMC_OBS_HEADER 8
+#define LQMC_OBS_LEN(n) (LQMC_OBS_HEADER + 2 * (n) + 2 * (n) * (n))
+
+/* per-chain diagnostics layout (lqmc_get_diagnostics), float64:
+ *   [0] accepted flips (cumulative)  [1] attempted flips (cumulative)
+ *   [2] max stabilisation residual max|G_wrapped - G_scratch| of the last launch
+ *   [3] log|det G_up|  [4] log|det G_dn|  [5] sign det G_up  [6] sign det G_dn
+ *   [7] sweeps done (cumulative; the philox sweep counter)                                */
+#define LQMC_DIAG_LEN 8
+
+typedef struct lqmc_params {
+    int32_t mode;          /* LQMC_MODE_*                                                  */
+    int32_t precision;     /* LQMC_PREC_*                                                  */
+    int32_t rng;           /* LQMC_RNG_*                                                   */
+    int32_t stab_every;    /* slices between from-scratch refreshes (dqmc); 0 -> 10        */
+    int32_t delay;         /* delayed-update depth k for LQMC_PREC_MIXED; 0 -> automatic   */
+    int32_t record;        /* 1: keep per-site accept decisions of the last lqmc_sweep    */
+    uint64_t seed;         /* Philox key word 0 (LQMC_RNG_PHILOX)                          */
+    int32_t device;        /* CUDA device ordinal                                          */
+    int32_t reserved[7];
+} lqmc_params;
+
+typedef struct lqmc_handle lqmc_handle;
+
+/* Create a handle.  Replaces the solver construction LatticeQMC.__init__
+ * (lqmc/lqmc.py:16-79) minus the model set-up, which stays on the host. */
+int lqmc_create(const lqmc_params* params, lqmc_handle** out);
+
+/* Define the batch of independent Markov chains (on-device replacement of the walker pool,
+ * lqmc/multiprocessing.py:252-289).  Chain c has n_sites[c] sites and n_slices[c] time
+ * slices; exp_k[c] = expm(-dtau K) (lqmc/lqmc.py:106), exp_k_inv[c] = its inverse used by
+ * the wrap (compat: numpy inv(exp_k); dqmc: expm(+dtau K)), kinetic[c] = K
+ * (lqmc/hubbard.py:91-110, used by the energy measurement), exp_consts[4c..4c+3] =
+ * {exp(2 lambda), exp(-2 lambda), exp(-lambda), exp(lambda)} (lqmc/lqmc.py:105, :149-154,
+ * :313-323) and u[c] the interaction.  Allocates every device buffer. */
+int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
+                    const int32_t* n_slices, const double* const* exp_k,
+                    const double* const* exp_k_inv, const double* const* kinetic,
+                    const double* exp_consts, const double* u);
+
+/* Upload / download the HS field of one chain, (n_sites, n_slices) int8 in {-1, +1}
+ * (Configuration.config, lqmc/configuration.py:86-136). */
+int lqmc_set_field(lqmc_handle* h, int32_t chain, const int8_t* field);
+int lqmc_get_field(lqmc_handle* h, int32_t chain, int8_t* field);
+
+/* Replay mode: the uniforms chain `chain` consumes in its next lqmc_sweep call, in sweep
+ * order (per sweep: l = L-1..0, i = 0..N-1), n_sweeps * N * L doubles.  Replaces the
+ * np.random.rand() draw per site (lqmc/lqmc.py:317). */
+int lqmc_set_uniforms(lqmc_handle* h, int32_t chain, const double* uniforms, size_t count);
+
+/* Run n_sweeps sweeps of every chain (lqmc/lqmc.py:301-347 per sweep; warmup_loop /
+ * measure_loop, :349-375).  measure != 0 accumulates G and the Wick observables after
+ * every sweep.  Asynchronous on `stream` (a cudaStream_t, NULL = default stream). */
+int lqmc_sweep(lqmc_handle* h, int32_t n_sweeps, int32_t measure, void* stream);
+
+/* Green's functions after the last sweep, (2, N, N): the value _update_step returns
+ * (lqmc/lqmc.py:347). */
+int lqmc_get_green(lqmc_handle* h, int32_t chain, double* green);
+
+/* Accumulated sum of G over measured sweeps, (2, N, N), and the number of measurements;
+ * sum / count is what measure_loop returns (lqmc/lqmc.py:356-375). */
+int lqmc_get_green_sum(lqmc_handle* h, int32_t chain, double* green_sum, int64_t* count);
+
+/* Accumulated Wick observables, LQMC_OBS_LEN(N) doubles (layout above). */
+int lqmc_get_observables(lqmc_handle* h, int32_t chain, double* obs);
+
+/* Clear the measurement accumulators of every chain. */
+int lqmc_reset_measurements(lqmc_handle* h);
+
+/* Per-site accept decisions of the last lqmc_sweep (params.record = 1), int8
+ * [n_sweeps][L][N] in sweep order (step = L-1-l); the decisions the reference logs per site
+ * (lqmc/lqmc.py:317, :335). */
+int lqmc_get_decisions(lqmc_handle* h, int32_t chain, int8_t* decisions, size_t count);
+
+/* Per-chain diagnostics, LQMC_DIAG_LEN doubles (layout above). */
+int lqmc_get_diagnostics(lqmc_handle* h, int32_t chain, double* diag);
+
+/* Per-chain LQMC_STATUS_* bit masks, n_chains int32 (0 = healthy). */
+int lqmc_get_status(lqmc_handle* h, int32_t* status);
+
+/* Device kernel launches issued by the last lqmc_sweep call. */
+int lqmc_get_launch_count(lqmc_handle* h, int64_t* launches);
+
+/* Message for the last failure on this handle (or for a failed lqmc_create when h == NULL). */
+const char* lqmc_last_error(const lqmc_handle* h);
+
+/* Release the handle and every device buffer it owns. */
+void lqmc_destroy(lqmc_handle* h);
+
+/* LQMC_ABI_VERSION of the loaded library. */
+int lqmc_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LQMC_GPU_H */

@@ -1,0 +1,126 @@
+"""ctypes binding of liblqmc_gpu.so (the C ABI in include/lqmc_gpu.h).
+
+The library is built in-tree by ``latticeqmc_gb300.build``.  There is no CPU fallback:
+if the library is missing or no CUDA device is present, loading or ``lqmc_create`` fails
+with an exception.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "liblqmc_gpu.so")
+
+LQMC_OK = 0
+ERRORS = {-1: "LQMC_ERR_INVALID", -2: "LQMC_ERR_CUDA", -3: "LQMC_ERR_STATE",
+          -4: "LQMC_ERR_UNSUPPORTED", -5: "LQMC_ERR_NUMERIC", -6: "LQMC_ERR_NOMEM"}
+MODES = {"compat": 0, "dqmc": 1}
+PRECISIONS = {"fp64": 0, "mixed": 1}
+RNGS = {"replay": 0, "philox": 1}
+STATUS_NONFINITE, STATUS_SINGULAR, STATUS_DRIFT = 1, 2, 4
+OBS_HEADER = 8
+DIAG_LEN = 8
+
+
+def obs_len(n):
+    return OBS_HEADER + 2 * n + 2 * n * n
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("mode", ctypes.c_int32), ("precision", ctypes.c_int32), ("rng", ctypes.c_int32),
+                ("stab_every", ctypes.c_int32), ("delay", ctypes.c_int32), ("record", ctypes.c_int32),
+                ("seed", ctypes.c_uint64), ("device", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 7)]
+
+
+class LqmcError(RuntimeError):
+    """A negative return code from liblqmc_gpu.so."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+# (name, restype, argtypes) of every exported symbol
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+_SIGS = [
+    ("lqmc_abi_version", ctypes.c_int, []),
+    ("lqmc_create", ctypes.c_int, [ctypes.POINTER(Params), ctypes.POINTER(_P)]),
+    ("lqmc_set_chains", ctypes.c_int, [_P, _I32, _P, _P, _P, _P, _P, _P, _P]),
+    ("lqmc_set_field", ctypes.c_int, [_P, _I32, _P]),
+    ("lqmc_get_field", ctypes.c_int, [_P, _I32, _P]),
+    ("lqmc_set_uniforms", ctypes.c_int, [_P, _I32, _P, ctypes.c_size_t]),
+    ("lqmc_sweep", ctypes.c_int, [_P, _I32, _I32, _P]),
+    ("lqmc_get_green", ctypes.c_int, [_P, _I32, _P]),
+    ("lqmc_get_green_sum", ctypes.c_int, [_P, _I32, _P, _P]),
+    ("lqmc_get_observables", ctypes.c_int, [_P, _I32, _P]),
+    ("lqmc_reset_measurements", ctypes.c_int, [_P]),
+    ("lqmc_get_decisions", ctypes.c_int, [_P, _I32, _P, ctypes.c_size_t]),
+    ("lqmc_get_diagnostics", ctypes.c_int, [_P, _I32, _P]),
+    ("lqmc_get_status", ctypes.c_int, [_P, _P]),
+    ("lqmc_get_launch_count", ctypes.c_int, [_P, _P]),
+    ("lqmc_last_error", ctypes.c_char_p, [_P]),
+    ("lqmc_destroy", None, [_P]),
+]
+EXPORTED = [s[0] for s in _SIGS]
+
+_lib = None
+
+
+def load():
+    """Load liblqmc_gpu.so once; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with "
+                               "`python -m latticeqmc_gb300.build` (no CPU fallback exists)")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, res, args in _SIGS:
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class Handle:
+    """Owns one lqmc_handle; every call checks the return code."""
+
+    def __init__(self, mode, precision, rng, stab_every, delay, seed, record, device):
+        self.lib = load()
+        p = Params(mode=MODES[mode], precision=PRECISIONS[precision], rng=RNGS[rng],
+                   stab_every=int(stab_every), delay=int(delay), record=int(bool(record)),
+                   seed=int(seed) & ((1 << 64) - 1), device=int(device))
+        h = ctypes.c_void_p()
+        rc = self.lib.lqmc_create(ctypes.byref(p), ctypes.byref(h))
+        if rc != LQMC_OK:
+            raise LqmcError(rc, self.lib.lqmc_last_error(None).decode())
+        self.h = h
+
+    def check(self, rc):
+        if rc != LQMC_OK:
+            raise LqmcError(rc, self.lib.lqmc_last_error(self.h).decode())
+
+    def call(self, name, *args):
+        self.check(getattr(self.lib, name)(self.h, *args))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.lqmc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def as_f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)

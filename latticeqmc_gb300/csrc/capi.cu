@@ -1,0 +1,513 @@
+// C ABI of liblqmc_gpu.so (declared in include/lqmc_gpu.h): handle, device memory, launches.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <functional>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "chain_desc.h"
+#include "lqmc_gpu.h"
+
+namespace lqmc {
+size_t sweep_fp64_smem_bytes(int n, int flags);
+cudaError_t launch_sweep_fp64(const ChainDesc* d_descs, int n_chains, size_t smem, int n_sweeps,
+                              int measure, cudaStream_t stream);
+}  // namespace lqmc
+
+using lqmc::ChainDesc;
+
+namespace {
+
+constexpr int kMaxSitesFp64 = 128;
+constexpr size_t kAlign = 32;   // doubles (256 bytes) between device sub-buffers
+
+std::string g_create_error;
+
+struct Bucket {
+    size_t smem = 0;
+    std::vector<int> chains;
+    ChainDesc* d_descs = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+};
+
+size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+}  // namespace
+
+struct lqmc_handle {
+    lqmc_params p{};
+    std::string err;
+    int n_chains = 0;
+    std::vector<ChainDesc> desc;
+    std::vector<char> field_set;
+    std::vector<double*> d_uni;
+    std::vector<size_t> uni_cap, uni_count;
+    double* d_f64 = nullptr;
+    int8_t* d_i8 = nullptr;
+    int32_t* d_status = nullptr;
+    int8_t* d_dec = nullptr;
+    size_t dec_cap = 0;
+    std::vector<Bucket> buckets;
+    cudaEvent_t fork = nullptr;
+    cudaStream_t last_stream = nullptr;
+    int last_sweeps = 0;
+    int64_t launches = 0;
+    bool descs_dirty = true;
+};
+
+namespace {
+
+int fail(lqmc_handle* h, int code, const std::string& msg) {
+    if (h) h->err = msg;
+    else g_create_error = msg;
+    return code;
+}
+
+int cuda_fail(lqmc_handle* h, cudaError_t e, const char* what) {
+    return fail(h, LQMC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define LQMC_CK(h, call)                                      \
+    do {                                                      \
+        cudaError_t e_ = (call);                              \
+        if (e_ != cudaSuccess) return cuda_fail((h), e_, #call); \
+    } while (0)
+
+void release(lqmc_handle* h) {
+    for (auto& b : h->buckets) {
+        if (b.d_descs) cudaFree(b.d_descs);
+        if (b.stream) cudaStreamDestroy(b.stream);
+        if (b.done) cudaEventDestroy(b.done);
+    }
+    h->buckets.clear();
+    for (double* u : h->d_uni)
+        if (u) cudaFree(u);
+    h->d_uni.clear();
+    if (h->d_f64) cudaFree(h->d_f64);
+    if (h->d_i8) cudaFree(h->d_i8);
+    if (h->d_status) cudaFree(h->d_status);
+    if (h->d_dec) cudaFree(h->d_dec);
+    h->d_f64 = nullptr;
+    h->d_i8 = nullptr;
+    h->d_status = nullptr;
+    h->d_dec = nullptr;
+    h->dec_cap = 0;
+    h->n_chains = 0;
+    h->desc.clear();
+}
+
+int check_chain(lqmc_handle* h, int32_t chain) {
+    if (!h) return LQMC_ERR_INVALID;
+    if (h->n_chains == 0) return fail(h, LQMC_ERR_STATE, "no chains defined (call lqmc_set_chains)");
+    if (chain < 0 || chain >= h->n_chains) return fail(h, LQMC_ERR_INVALID, "chain index out of range");
+    return LQMC_OK;
+}
+
+int sync_last(lqmc_handle* h) {
+    cudaError_t e = h->last_stream ? cudaStreamSynchronize(h->last_stream) : cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(h, e, "synchronize");
+    return LQMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lqmc_abi_version(void) { return LQMC_ABI_VERSION; }
+
+int lqmc_create(const lqmc_params* params, lqmc_handle** out) {
+    if (!params || !out) return fail(nullptr, LQMC_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (params->mode != LQMC_MODE_COMPAT && params->mode != LQMC_MODE_DQMC)
+        return fail(nullptr, LQMC_ERR_INVALID, "unknown mode");
+    if (params->precision != LQMC_PREC_FP64 && params->precision != LQMC_PREC_MIXED)
+        return fail(nullptr, LQMC_ERR_INVALID, "unknown precision");
+    if (params->rng != LQMC_RNG_REPLAY && params->rng != LQMC_RNG_PHILOX)
+        return fail(nullptr, LQMC_ERR_INVALID, "unknown rng");
+    if (params->stab_every < 0 || params->delay < 0)
+        return fail(nullptr, LQMC_ERR_INVALID, "negative stab_every or delay");
+    if (params->precision == LQMC_PREC_MIXED && params->mode == LQMC_MODE_COMPAT)
+        return fail(nullptr, LQMC_ERR_UNSUPPORTED, "compat mode replays float64 arithmetic only");
+    if (params->precision == LQMC_PREC_MIXED)
+        return fail(nullptr, LQMC_ERR_UNSUPPORTED, "mixed precision is not available in this build");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess) return fail(nullptr, LQMC_ERR_CUDA, std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e));
+    if (params->device < 0 || params->device >= ndev) return fail(nullptr, LQMC_ERR_INVALID, "device ordinal out of range");
+    e = cudaSetDevice(params->device);
+    if (e != cudaSuccess) return fail(nullptr, LQMC_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    lqmc_handle* h = new lqmc_handle();
+    h->p = *params;
+    if (h->p.stab_every == 0) h->p.stab_every = 10;
+    e = cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        delete h;
+        return fail(nullptr, LQMC_ERR_CUDA, std::string("cudaEventCreate: ") + cudaGetErrorString(e));
+    }
+    *out = h;
+    return LQMC_OK;
+}
+
+int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
+                    const int32_t* n_slices, const double* const* exp_k,
+                    const double* const* exp_k_inv, const double* const* kinetic,
+                    const double* exp_consts, const double* u) {
+    if (!h) return LQMC_ERR_INVALID;
+    if (n_chains <= 0 || !n_sites || !n_slices || !exp_k || !exp_k_inv || !kinetic || !exp_consts || !u)
+        return fail(h, LQMC_ERR_INVALID, "lqmc_set_chains: null argument or n_chains <= 0");
+    LQMC_CK(h, cudaSetDevice(h->p.device));
+    for (int c = 0; c < n_chains; ++c) {
+        if (n_sites[c] < 1 || n_slices[c] < 1)
+            return fail(h, LQMC_ERR_INVALID, "chain " + std::to_string(c) + ": n_sites and n_slices must be >= 1");
+        if (n_sites[c] > kMaxSitesFp64)
+            return fail(h, LQMC_ERR_UNSUPPORTED, "chain " + std::to_string(c) + ": n_sites > 128 needs the tiled engine");
+        if (!exp_k[c] || !exp_k_inv[c] || !kinetic[c])
+            return fail(h, LQMC_ERR_INVALID, "chain " + std::to_string(c) + ": null matrix");
+    }
+    release(h);
+    int dev = h->p.device;
+    int optin = 0;
+    LQMC_CK(h, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    const size_t smem_cap = (size_t)optin - 1024;   // static shared memory of the kernel
+
+    h->n_chains = n_chains;
+    h->desc.assign(n_chains, ChainDesc{});
+    h->field_set.assign(n_chains, 0);
+    h->d_uni.assign(n_chains, nullptr);
+    h->uni_cap.assign(n_chains, 0);
+    h->uni_count.assign(n_chains, 0);
+
+    // layout of the float64 arena
+    std::vector<size_t> off(n_chains);
+    std::vector<size_t> smem(n_chains);
+    size_t total = 0, total_i8 = 0;
+    std::vector<size_t> off_i8(n_chains);
+    for (int c = 0; c < n_chains; ++c) {
+        ChainDesc& d = h->desc[c];
+        const int n = n_sites[c], L = n_slices[c];
+        const size_t nn = (size_t)n * n;
+        d.n = n;
+        d.L = L;
+        d.mode = h->p.mode;
+        d.rng = h->p.rng;
+        d.stab_every = std::min(h->p.stab_every, L);
+        d.n_chunks = (h->p.mode == LQMC_MODE_DQMC) ? (L + d.stab_every - 1) / d.stab_every : 0;
+        d.chain_id = c;
+        d.seed = h->p.seed;
+        d.slot = (int32_t)round_up(2 * nn + n + 1, 4);
+        for (int k = 0; k < 4; ++k) d.c[k] = exp_consts[4 * c + k];
+        d.u = u[c];
+        d.drift_tol = 1e-6;
+        int flags = 0;
+        if (lqmc::sweep_fp64_smem_bytes(n, flags) > smem_cap) flags = lqmc::kScratchInGlobal;
+        if (lqmc::sweep_fp64_smem_bytes(n, flags) > smem_cap) flags |= lqmc::kGreenInGlobal;
+        d.flags = flags;
+        smem[c] = lqmc::sweep_fp64_smem_bytes(n, flags);
+        size_t work = (size_t)(2 * d.n_chunks + 4) * d.slot;
+        if (flags & lqmc::kGreenInGlobal) work += 2 * nn;
+        if (flags & lqmc::kScratchInGlobal) work += 2 * nn;
+        const size_t need = round_up(nn, kAlign) * 5 + round_up(2 * nn, kAlign) * 2 +
+                            round_up(LQMC_OBS_LEN(n), kAlign) + round_up(LQMC_DIAG_LEN, kAlign) +
+                            round_up(work, kAlign);
+        off[c] = total;
+        total += need;
+        off_i8[c] = total_i8;
+        total_i8 += round_up((size_t)n * L, 256);
+    }
+    cudaError_t e = cudaMalloc(&h->d_f64, total * sizeof(double));
+    if (e != cudaSuccess) { release(h); return fail(h, LQMC_ERR_NOMEM, "device allocation of " + std::to_string(total * 8) + " bytes failed"); }
+    e = cudaMalloc(&h->d_i8, total_i8);
+    if (e != cudaSuccess) { release(h); return fail(h, LQMC_ERR_NOMEM, "device allocation of the fields failed"); }
+    e = cudaMalloc(&h->d_status, sizeof(int32_t) * n_chains);
+    if (e != cudaSuccess) { release(h); return fail(h, LQMC_ERR_NOMEM, "device allocation of the status words failed"); }
+    LQMC_CK(h, cudaMemset(h->d_f64, 0, total * sizeof(double)));
+    LQMC_CK(h, cudaMemset(h->d_i8, 1, total_i8));
+    LQMC_CK(h, cudaMemset(h->d_status, 0, sizeof(int32_t) * n_chains));
+
+    std::vector<double> tmp;
+    for (int c = 0; c < n_chains; ++c) {
+        ChainDesc& d = h->desc[c];
+        const int n = d.n;
+        const size_t nn = (size_t)n * n;
+        double* p = h->d_f64 + off[c];
+        auto take = [&](size_t count) { double* r = p; p += round_up(count, kAlign); return r; };
+        double* ek = take(nn);
+        double* ekt = take(nn);
+        double* eki = take(nn);
+        double* ekit = take(nn);
+        double* kin = take(nn);
+        d.green = take(2 * nn);
+        d.gsum = take(2 * nn);
+        d.obs = take(LQMC_OBS_LEN(n));
+        d.diag = take(LQMC_DIAG_LEN);
+        d.work = p;
+        d.expk = ek;
+        d.expkT = ekt;
+        d.expkinv = eki;
+        d.expkinvT = ekit;
+        d.kinetic = kin;
+        d.field = h->d_i8 + off_i8[c];
+        d.status = h->d_status + c;
+        tmp.resize(nn);
+        LQMC_CK(h, cudaMemcpy(ek, exp_k[c], nn * sizeof(double), cudaMemcpyHostToDevice));
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) tmp[(size_t)j * n + i] = exp_k[c][(size_t)i * n + j];
+        LQMC_CK(h, cudaMemcpy(ekt, tmp.data(), nn * sizeof(double), cudaMemcpyHostToDevice));
+        LQMC_CK(h, cudaMemcpy(eki, exp_k_inv[c], nn * sizeof(double), cudaMemcpyHostToDevice));
+        for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) tmp[(size_t)j * n + i] = exp_k_inv[c][(size_t)i * n + j];
+        LQMC_CK(h, cudaMemcpy(ekit, tmp.data(), nn * sizeof(double), cudaMemcpyHostToDevice));
+        LQMC_CK(h, cudaMemcpy(kin, kinetic[c], nn * sizeof(double), cudaMemcpyHostToDevice));
+    }
+
+    // buckets of equal shared-memory footprint, largest first
+    std::map<size_t, std::vector<int>, std::greater<size_t>> groups;
+    for (int c = 0; c < n_chains; ++c) groups[smem[c]].push_back(c);
+    for (auto& kv : groups) {
+        Bucket b;
+        b.smem = kv.first;
+        b.chains = kv.second;
+        e = cudaMalloc(&b.d_descs, sizeof(ChainDesc) * b.chains.size());
+        if (e != cudaSuccess) { h->buckets.push_back(b); release(h); return fail(h, LQMC_ERR_NOMEM, "descriptor allocation failed"); }
+        e = cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b.done, cudaEventDisableTiming);
+        h->buckets.push_back(b);
+        if (e != cudaSuccess) { release(h); return cuda_fail(h, e, "bucket stream/event"); }
+    }
+    h->descs_dirty = true;
+    return LQMC_OK;
+}
+
+int lqmc_set_field(lqmc_handle* h, int32_t chain, const int8_t* field) {
+    int rc = check_chain(h, chain);
+    if (rc) return rc;
+    if (!field) return fail(h, LQMC_ERR_INVALID, "null field");
+    const ChainDesc& d = h->desc[chain];
+    std::vector<int8_t> t((size_t)d.n * d.L);
+    for (int i = 0; i < d.n; ++i)
+        for (int l = 0; l < d.L; ++l) {
+            const int8_t v = field[(size_t)i * d.L + l];
+            if (v != 1 && v != -1) return fail(h, LQMC_ERR_INVALID, "field values must be +1 or -1");
+            t[(size_t)l * d.n + i] = v;
+        }
+    {
+        const int r = sync_last(h);
+        if (r) return r;
+    }
+    LQMC_CK(h, cudaMemcpy(d.field, t.data(), t.size(), cudaMemcpyHostToDevice));
+    h->field_set[chain] = 1;
+    return LQMC_OK;
+}
+
+int lqmc_get_field(lqmc_handle* h, int32_t chain, int8_t* field) {
+    int rc = check_chain(h, chain);
+    if (rc) return rc;
+    if (!field) return fail(h, LQMC_ERR_INVALID, "null field");
+    if ((rc = sync_last(h))) return rc;
+    const ChainDesc& d = h->desc[chain];
+    std::vector<int8_t> t((size_t)d.n * d.L);
+    LQMC_CK(h, cudaMemcpy(t.data(), d.field, t.size(), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < d.n; ++i)
+        for (int l = 0; l < d.L; ++l) field[(size_t)i * d.L + l] = t[(size_t)l * d.n + i];
+    return LQMC_OK;
+}
+
+int lqmc_set_uniforms(lqmc_handle* h, int32_t chain, const double* uniforms, size_t count) {
+    int rc = check_chain(h, chain);
+    if (rc) return rc;
+    if (h->p.rng != LQMC_RNG_REPLAY) return fail(h, LQMC_ERR_STATE, "uniforms are only uploaded in replay mode");
+    if (!uniforms && count) return fail(h, LQMC_ERR_INVALID, "null uniforms");
+    const ChainDesc& d = h->desc[chain];
+    const size_t per = (size_t)d.n * d.L;
+    if (count % per) return fail(h, LQMC_ERR_INVALID, "uniform count must be a multiple of n_sites * n_slices");
+    if ((rc = sync_last(h))) return rc;
+    if (count > h->uni_cap[chain]) {
+        if (h->d_uni[chain]) cudaFree(h->d_uni[chain]);
+        h->d_uni[chain] = nullptr;
+        h->uni_cap[chain] = 0;
+        cudaError_t e = cudaMalloc(&h->d_uni[chain], count * sizeof(double));
+        if (e != cudaSuccess) return fail(h, LQMC_ERR_NOMEM, "uniform buffer allocation failed");
+        h->uni_cap[chain] = count;
+        h->descs_dirty = true;
+    }
+    if (count) LQMC_CK(h, cudaMemcpy(h->d_uni[chain], uniforms, count * sizeof(double), cudaMemcpyHostToDevice));
+    h->uni_count[chain] = count;
+    if (h->desc[chain].uniforms != h->d_uni[chain]) {
+        h->desc[chain].uniforms = h->d_uni[chain];
+        h->descs_dirty = true;
+    }
+    return LQMC_OK;
+}
+
+int lqmc_sweep(lqmc_handle* h, int32_t n_sweeps, int32_t measure, void* stream_ptr) {
+    if (!h) return LQMC_ERR_INVALID;
+    if (h->n_chains == 0) return fail(h, LQMC_ERR_STATE, "no chains defined (call lqmc_set_chains)");
+    if (n_sweeps < 0) return fail(h, LQMC_ERR_INVALID, "n_sweeps < 0");
+    h->launches = 0;
+    if (n_sweeps == 0) return LQMC_OK;
+    cudaStream_t stream = (cudaStream_t)stream_ptr;
+    for (int c = 0; c < h->n_chains; ++c) {
+        if (!h->field_set[c]) return fail(h, LQMC_ERR_STATE, "chain " + std::to_string(c) + ": field not set");
+        if (h->p.rng == LQMC_RNG_REPLAY) {
+            const size_t need = (size_t)n_sweeps * h->desc[c].n * h->desc[c].L;
+            if (h->uni_count[c] < need)
+                return fail(h, LQMC_ERR_STATE, "chain " + std::to_string(c) + ": fewer uniforms uploaded than the sweeps consume");
+        }
+    }
+    int rec = h->p.record ? 1 : 0;
+    if (rec) {
+        size_t need = 0;
+        for (auto& d : h->desc) need += round_up((size_t)n_sweeps * d.L * d.n, 256);
+        if (need > h->dec_cap) {
+            if (h->d_dec) cudaFree(h->d_dec);
+            h->d_dec = nullptr;
+            h->dec_cap = 0;
+            cudaError_t e = cudaMalloc(&h->d_dec, need);
+            if (e != cudaSuccess) return fail(h, LQMC_ERR_NOMEM, "decision buffer allocation failed");
+            h->dec_cap = need;
+        }
+        size_t o = 0;
+        for (auto& d : h->desc) {
+            if (d.decisions != h->d_dec + o) h->descs_dirty = true;
+            d.decisions = h->d_dec + o;
+            o += round_up((size_t)n_sweeps * d.L * d.n, 256);
+        }
+    }
+    for (auto& d : h->desc) {
+        if (d.record != rec) { d.record = rec; h->descs_dirty = true; }
+    }
+    if (h->descs_dirty) {
+        const int r = sync_last(h);
+        if (r) return r;
+        std::vector<ChainDesc> tmp;
+        for (auto& b : h->buckets) {
+            tmp.clear();
+            for (int c : b.chains) tmp.push_back(h->desc[c]);
+            LQMC_CK(h, cudaMemcpy(b.d_descs, tmp.data(), sizeof(ChainDesc) * tmp.size(), cudaMemcpyHostToDevice));
+        }
+        h->descs_dirty = false;
+    }
+    if (h->buckets.size() == 1) {
+        Bucket& b = h->buckets[0];
+        LQMC_CK(h, lqmc::launch_sweep_fp64(b.d_descs, (int)b.chains.size(), b.smem, n_sweeps, measure, stream));
+        ++h->launches;
+    } else {
+        LQMC_CK(h, cudaEventRecord(h->fork, stream));
+        for (auto& b : h->buckets) {
+            LQMC_CK(h, cudaStreamWaitEvent(b.stream, h->fork, 0));
+            LQMC_CK(h, lqmc::launch_sweep_fp64(b.d_descs, (int)b.chains.size(), b.smem, n_sweeps, measure, b.stream));
+            LQMC_CK(h, cudaEventRecord(b.done, b.stream));
+            LQMC_CK(h, cudaStreamWaitEvent(stream, b.done, 0));
+            ++h->launches;
+        }
+    }
+    if (h->p.rng == LQMC_RNG_REPLAY)
+        for (int c = 0; c < h->n_chains; ++c) h->uni_count[c] = 0;
+    h->last_stream = stream;
+    h->last_sweeps = n_sweeps;
+    return LQMC_OK;
+}
+
+int lqmc_get_green(lqmc_handle* h, int32_t chain, double* green) {
+    int rc = check_chain(h, chain);
+    if (rc) return rc;
+    if (!green) return fail(h, LQMC_ERR_INVALID, "null output");
+    if ((rc = sync_last(h))) return rc;
+    const ChainDesc& d = h->desc[chain];
+    LQMC_CK(h, cudaMemcpy(green, d.green, 2 * (size_t)d.n * d.n * sizeof(double), cudaMemcpyDeviceToHost));
+    return LQMC_OK;
+}
+
+int lqmc_get_green_sum(lqmc_handle* h, int32_t chain, double* green_sum, int64_t* count) {
+    int rc = check_chain(h, chain);
+    if (rc) return rc;
+    if ((rc = sync_last(h))) return rc;
+    const ChainDesc& d = h->desc[chain];
+    if (green_sum)
+        LQMC_CK(h, cudaMemcpy(green_sum, d.gsum, 2 * (size_t)d.n * d.n * sizeof(double), cudaMemcpyDeviceToHost));
+    if (count) {
+        double c = 0.0;
+        LQMC_CK(h, cudaMemcpy(&c, d.obs, sizeof(double), cudaMemcpyDeviceToHost));
+        *count = (int64_t)c;
+    }
+    return LQMC_OK;
+}
+
+int lqmc_get_observables(lqmc_handle* h, int32_t chain, double* obs) {
+    int rc = check_chain(h, chain);
+    if (rc) return rc;
+    if (!obs) return fail(h, LQMC_ERR_INVALID, "null output");
+    if ((rc = sync_last(h))) return rc;
+    const ChainDesc& d = h->desc[chain];
+    LQMC_CK(h, cudaMemcpy(obs, d.obs, LQMC_OBS_LEN(d.n) * sizeof(double), cudaMemcpyDeviceToHost));
+    return LQMC_OK;
+}
+
+int lqmc_reset_measurements(lqmc_handle* h) {
+    if (!h) return LQMC_ERR_INVALID;
+    if (h->n_chains == 0) return fail(h, LQMC_ERR_STATE, "no chains defined");
+    int rc = sync_last(h);
+    if (rc) return rc;
+    for (auto& d : h->desc) {
+        LQMC_CK(h, cudaMemset(d.gsum, 0, 2 * (size_t)d.n * d.n * sizeof(double)));
+        LQMC_CK(h, cudaMemset(d.obs, 0, LQMC_OBS_LEN(d.n) * sizeof(double)));
+    }
+    return LQMC_OK;
+}
+
+int lqmc_get_decisions(lqmc_handle* h, int32_t chain, int8_t* decisions, size_t count) {
+    int rc = check_chain(h, chain);
+    if (rc) return rc;
+    if (!h->p.record) return fail(h, LQMC_ERR_STATE, "handle was created with record = 0");
+    const ChainDesc& d = h->desc[chain];
+    const size_t have = (size_t)h->last_sweeps * d.L * d.n;
+    if (!decisions || count < have) return fail(h, LQMC_ERR_INVALID, "decision buffer too small");
+    if ((rc = sync_last(h))) return rc;
+    if (have) LQMC_CK(h, cudaMemcpy(decisions, d.decisions, have, cudaMemcpyDeviceToHost));
+    return LQMC_OK;
+}
+
+int lqmc_get_diagnostics(lqmc_handle* h, int32_t chain, double* diag) {
+    int rc = check_chain(h, chain);
+    if (rc) return rc;
+    if (!diag) return fail(h, LQMC_ERR_INVALID, "null output");
+    if ((rc = sync_last(h))) return rc;
+    LQMC_CK(h, cudaMemcpy(diag, h->desc[chain].diag, LQMC_DIAG_LEN * sizeof(double), cudaMemcpyDeviceToHost));
+    return LQMC_OK;
+}
+
+int lqmc_get_status(lqmc_handle* h, int32_t* status) {
+    if (!h) return LQMC_ERR_INVALID;
+    if (h->n_chains == 0) return fail(h, LQMC_ERR_STATE, "no chains defined");
+    if (!status) return fail(h, LQMC_ERR_INVALID, "null output");
+    int rc = sync_last(h);
+    if (rc) return rc;
+    LQMC_CK(h, cudaMemcpy(status, h->d_status, sizeof(int32_t) * h->n_chains, cudaMemcpyDeviceToHost));
+    return LQMC_OK;
+}
+
+int lqmc_get_launch_count(lqmc_handle* h, int64_t* launches) {
+    if (!h || !launches) return LQMC_ERR_INVALID;
+    *launches = h->launches;
+    return LQMC_OK;
+}
+
+const char* lqmc_last_error(const lqmc_handle* h) {
+    return h ? h->err.c_str() : g_create_error.c_str();
+}
+
+void lqmc_destroy(lqmc_handle* h) {
+    if (!h) return;
+    cudaSetDevice(h->p.device);
+    cudaDeviceSynchronize();
+    release(h);
+    if (h->fork) cudaEventDestroy(h->fork);
+    delete h;
+}
+
+}  // extern "C"

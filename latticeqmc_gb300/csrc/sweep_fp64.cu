@@ -1,0 +1,581 @@
+// Persistent float64 sweep kernel: one CTA per Markov chain, G_up / G_dn held in shared
+// memory (n <= 90 with scratch, n <= 120 without), for both algorithm modes.
+//
+// Hot path of lqmc/lqmc.py:301-347 (fast sweep) restated per chain:
+//   K1 ratio + accept      lqmc.py:313-317          every thread evaluates it redundantly
+//   K2 rank-1 update       lqmc.py:318-333          block-wide, in place in shared memory
+//   K3 slice wrap          lqmc.py:337-345          two in-place GEMMs (column-/row-local)
+//   K4/K5 recompute of G   lqmc.py:156-185, :303-307
+//        compat: unstabilised B-chain product + LU inverse (the reference's arithmetic)
+//        dqmc:   pre-pivoted QR (UDT) chain product, right stack + left product,
+//                refreshed every stab_every slices, with log|det G| and sign
+//   K7 measurements        lqmc.py:356-375 (sum of G) + Wick observables
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "block_fp64.cuh"
+#include "chain_desc.h"
+#include "philox.cuh"
+#include "lqmc_gpu.h"
+
+namespace lqmc {
+namespace {
+
+using namespace blk;
+
+struct Smem {
+    double* g[2];
+    double* s0;
+    double* s1;
+    double* xv[2];
+    double* yv[2];
+    double* ev;
+    double* nrm;
+    double* tau;
+    double* dv;
+    int* order;
+    double* sv;     // kNW + 8 scalars
+};
+
+__device__ __forceinline__ double* slot_u(const ChainDesc& d, int idx) { return d.work + (size_t)idx * d.slot; }
+__device__ __forceinline__ double* slot_t(const ChainDesc& d, int idx) { return slot_u(d, idx) + d.n * d.n; }
+__device__ __forceinline__ double* slot_d(const ChainDesc& d, int idx) { return slot_u(d, idx) + 2 * d.n * d.n; }
+__device__ __forceinline__ double* slot_sign(const ChainDesc& d, int idx) { return slot_d(d, idx) + d.n; }
+// right stack slot of spin s, chunk c; left ping-pong slot p of spin s
+__device__ __forceinline__ int right_slot(const ChainDesc& d, int s, int c) { return s * d.n_chunks + c; }
+__device__ __forceinline__ int left_slot(const ChainDesc& d, int s, int p) { return 2 * d.n_chunks + 2 * s + p; }
+
+// ev[j] = exp(-sigma lambda s[j, l])  (lqmc.py:149-154), from the host-computed constants
+__device__ __forceinline__ void load_ev(const ChainDesc& d, double* ev, int l, int sigma) {
+    const int8_t* f = d.field + (size_t)l * d.n;
+    for (int j = threadIdx.x; j < d.n; j += kNT) ev[j] = (sigma * f[j] > 0) ? d.c[2] : d.c[3];
+}
+
+// ---------------------------------------------------------------------------------------
+// compat mode: the reference's arithmetic
+// ---------------------------------------------------------------------------------------
+
+// G_s = inv(1 + b_{L-1} ... b_0), b_l = exp_k diag(exp_v(l))   (lqmc.py:156-185, :303-307)
+__device__ void compat_recompute(const ChainDesc& d, Smem& sm, int s, int* singular) {
+    const int n = d.n, nn = n * n, sigma = s ? -1 : 1;
+    double* x = sm.s1;
+    double* b = sm.s0;
+    load_ev(d, sm.ev, d.L - 1, sigma);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nn; e += kNT) x[e] = __dmul_rn(d.expk[e], sm.ev[e % n]);
+    __syncthreads();
+    for (int l = d.L - 2; l >= 0; --l) {
+        load_ev(d, sm.ev, l, sigma);
+        __syncthreads();
+        for (int e = threadIdx.x; e < nn; e += kNT) b[e] = __dmul_rn(d.expk[e], sm.ev[e % n]);
+        __syncthreads();
+        gemm_right_inplace(x, b, n);
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < n; i += kNT) x[i * n + i] = __dadd_rn(1.0, x[i * n + i]);
+    set_identity(sm.g[s], n);
+    __syncthreads();
+    double la, sg;
+    int sing;
+    lu_solve(x, sm.g[s], n, sm.sv, &la, &sg, &sing);
+    if (sing) *singular = 1;
+    __syncthreads();
+}
+
+// G <- b G inv(b), b = diag(exp_v(l-1)) exp_k   (lqmc.py:339-345)
+__device__ void compat_wrap(const ChainDesc& d, Smem& sm, int l_next) {
+    const int n = d.n, nn = n * n;
+    for (int s = 0; s < 2; ++s) {
+        const int sigma = s ? -1 : 1;
+        load_ev(d, sm.ev, l_next, sigma);
+        __syncthreads();
+        for (int e = threadIdx.x; e < nn; e += kNT) {
+            const int m = e / n, j = e % n;
+            sm.s0[e] = __dmul_rn(sm.ev[j], d.expkT[e]);            // b^T[m][j] = d_j expK[j][m]
+            sm.s1[e] = __ddiv_rn(d.expkinv[e], sm.ev[j]);          // inv(b)[m][k] = expK^-1[m][k] / d_k
+            (void)m;
+        }
+        __syncthreads();
+        gemm_left_inplace(sm.g[s], sm.s0, n);
+        __syncthreads();
+        gemm_right_inplace(sm.g[s], sm.s1, n);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// dqmc mode: UDT chain products
+// ---------------------------------------------------------------------------------------
+
+// z holds C U_old.  Writes the UDT of C U_old diag(d_old) T_old (pre-pivoted QR).
+// d_old == nullptr / t_old == nullptr stand for ones / identity.  Returns det sign of U.
+__device__ double udt_absorb(const ChainDesc& d, Smem& sm, double* z, double* s,
+                             const double* d_old, const double* t_old,
+                             double* u_new, double* d_new, double* t_new) {
+    const int n = d.n, nn = n * n, lane = lane_id();
+    if (d_old) {
+        for (int e = threadIdx.x; e < nn; e += kNT) z[e] = z[e] * d_old[e % n];
+        __syncthreads();
+    }
+    for (int k = warp_id(); k < n; k += kNW) {
+        double acc = 0.0;
+        for (int i = lane; i < n; i += 32) { const double v = z[i * n + k]; acc = fma(v, v, acc); }
+        acc = warp_sum(acc);
+        if (lane == 0) sm.nrm[k] = sqrt(acc);
+    }
+    __syncthreads();
+    // rank by descending norm, ties by index; NaN sorts last so the ranks always form a
+    // permutation of 0..n-1
+    for (int k = threadIdx.x; k < n; k += kNT) {
+        const double v = isnan(sm.nrm[k]) ? -1.0 : sm.nrm[k];
+        int rank = 0;
+        for (int j = 0; j < n; ++j) {
+            const double w = isnan(sm.nrm[j]) ? -1.0 : sm.nrm[j];
+            rank += (w > v) || (w == v && j < k);
+        }
+        sm.order[rank] = k;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nn; e += kNT) {
+        const int i = e / n, r = e % n;
+        s[e] = z[i * n + sm.order[r]];
+    }
+    __syncthreads();
+    const int nrefl = householder_qr(s, sm.tau, n, sm.sv);
+    for (int i = threadIdx.x; i < n; i += kNT) {
+        const double di = s[i * n + i];
+        sm.dv[i] = di;
+        d_new[i] = di;
+    }
+    __syncthreads();
+    householder_form_q(u_new, s, sm.tau, n);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nn; e += kNT) {
+        const int i = e / n, k = e % n;
+        if (k >= i) s[e] = s[e] / sm.dv[i];
+    }
+    __syncthreads();
+    for (int i = warp_id(); i < n; i += kNW) {
+        for (int c = lane; c < n; c += 32) {
+            double acc = 0.0;
+            for (int k = i; k < n; ++k) {
+                const int src = sm.order[k];
+                const double tv = t_old ? t_old[src * n + c] : (src == c ? 1.0 : 0.0);
+                acc = fma(s[i * n + k], tv, acc);
+            }
+            t_new[i * n + c] = acc;
+        }
+    }
+    __syncthreads();
+    return (nrefl & 1) ? -1.0 : 1.0;
+}
+
+// G = (1 + U_R D_R T_R T_L^T D_L U_L^T)^-1 via the split D = D_big D_small.
+// ul == nullptr: the left product is the identity.  Writes G into g; returns the
+// residual max|G_new - G_old| when `residual`.
+__device__ double green_udt(const ChainDesc& d, Smem& sm, const double* ur, const double* dr,
+                            const double* tr, double sign_r, const double* ul,
+                            const double* dl, const double* tl, double sign_l, double* g,
+                            bool residual, double* logdet, double* sgn, int* singular) {
+    const int n = d.n, nn = n * n;
+    double* dbr = sm.xv[0];
+    double* dsr = sm.xv[1];
+    double* dbl = sm.yv[0];
+    double* dsl = sm.yv[1];
+    for (int i = threadIdx.x; i < n; i += kNT) {
+        const double a = dr[i];
+        const double b = fmax(fabs(a), 1.0);
+        dbr[i] = b;
+        dsr[i] = a / b;
+        if (ul) {
+            const double c = dl[i];
+            const double e = fmax(fabs(c), 1.0);
+            dbl[i] = e;
+            dsl[i] = c / e;
+        } else {
+            dbl[i] = 1.0;
+            dsl[i] = 1.0;
+        }
+    }
+    if (ul) {
+        gemm<true, false>(sm.s0, ur, ul, n);   // X = U_R^T U_L
+        gemm<false, true>(sm.s1, tr, tl, n);   // Y = T_R T_L^T
+    } else {
+        for (int e = threadIdx.x; e < nn; e += kNT) {
+            const int i = e / n, j = e % n;
+            sm.s0[e] = ur[j * n + i];
+            sm.s1[e] = tr[e];
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nn; e += kNT) {
+        const int i = e / n, j = e % n;
+        sm.s0[e] = sm.s0[e] / dbr[i] / dbl[j] + dsr[i] * sm.s1[e] * dsl[j];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nn; e += kNT) {
+        const int i = e / n, j = e % n;
+        sm.s1[e] = ur[j * n + i] / dbr[i];
+    }
+    __syncthreads();
+    double la, sw;
+    int sing;
+    lu_solve(sm.s0, sm.s1, n, sm.sv, &la, &sw, &sing);
+    if (sing) *singular = 1;
+    const double* src = sm.s1;
+    if (ul) {
+        for (int e = threadIdx.x; e < nn; e += kNT) sm.s1[e] = sm.s1[e] / dbl[e / n];
+        __syncthreads();
+        gemm<false, false>(sm.s0, ul, sm.s1, n);
+        __syncthreads();
+        src = sm.s0;
+    }
+    double res = 0.0;
+    if (residual) {
+        double m = 0.0;
+        for (int e = threadIdx.x; e < nn; e += kNT) m = fmax(m, fabs(src[e] - g[e]));
+        res = block_max(m, sm.sv);
+    }
+    // log|det G| = -(sum log D_big_R + log|det W| + sum log D_big_L)
+    double part = 0.0;
+    for (int i = threadIdx.x; i < n; i += kNT) part += log(dbr[i]) + log(dbl[i]);
+    const double tot = block_sum(part, sm.sv);
+    for (int e = threadIdx.x; e < nn; e += kNT) g[e] = src[e];
+    __syncthreads();
+    *logdet = -(tot + la);
+    *sgn = sign_r * sw * sign_l;
+    return res;
+}
+
+__device__ void dqmc_right_stack(const ChainDesc& d, Smem& sm, int s, double* logdet,
+                                 double* sgn, int* singular) {
+    const int n = d.n, nn = n * n, sigma = s ? -1 : 1;
+    for (int c = 0; c < d.n_chunks; ++c) {
+        const int lo = c * d.stab_every;
+        const int hi = min(lo + d.stab_every, d.L);
+        if (c == 0) set_identity(sm.s0, n);
+        else copy(sm.s0, slot_u(d, right_slot(d, s, c - 1)), nn);
+        __syncthreads();
+        for (int l = lo; l < hi; ++l) {
+            gemm_left_inplace(sm.s0, d.expkT, n);          // expK Z
+            load_ev(d, sm.ev, l, sigma);
+            __syncthreads();
+            for (int e = threadIdx.x; e < nn; e += kNT) sm.s0[e] = sm.ev[e / n] * sm.s0[e];
+            __syncthreads();
+        }
+        const int prev = right_slot(d, s, c - 1), cur = right_slot(d, s, c);
+        const double sg = udt_absorb(d, sm, sm.s0, sm.s1, c ? slot_d(d, prev) : nullptr,
+                                     c ? slot_t(d, prev) : nullptr, slot_u(d, cur),
+                                     slot_d(d, cur), slot_t(d, cur));
+        if (threadIdx.x == 0) *slot_sign(d, cur) = sg;
+        __syncthreads();
+    }
+    const int top = right_slot(d, s, d.n_chunks - 1);
+    green_udt(d, sm, slot_u(d, top), slot_d(d, top), slot_t(d, top), *slot_sign(d, top),
+              nullptr, nullptr, nullptr, 1.0, sm.g[s], false, logdet, sgn, singular);
+}
+
+// Left product of the chunk [lo, hi) on top of the left ping-pong slot `p_in`
+// (first == true: start from the identity); result into slot 1 - p_in.
+__device__ void dqmc_left_step(const ChainDesc& d, Smem& sm, int s, int p_in, bool first,
+                               int lo, int hi) {
+    const int n = d.n, nn = n * n, sigma = s ? -1 : 1;
+    const int in = left_slot(d, s, p_in), out = left_slot(d, s, 1 - p_in);
+    if (first) set_identity(sm.s0, n);
+    else copy(sm.s0, slot_u(d, in), nn);
+    __syncthreads();
+    for (int l = hi - 1; l >= lo; --l) {
+        load_ev(d, sm.ev, l, sigma);
+        __syncthreads();
+        for (int e = threadIdx.x; e < nn; e += kNT) sm.s0[e] = sm.ev[e / n] * sm.s0[e];
+        __syncthreads();
+        gemm_left_inplace(sm.s0, d.expk, n);            // expK^T (exp_v Z)
+        __syncthreads();
+    }
+    const double sg = udt_absorb(d, sm, sm.s0, sm.s1, first ? nullptr : slot_d(d, in),
+                                 first ? nullptr : slot_t(d, in), slot_u(d, out),
+                                 slot_d(d, out), slot_t(d, out));
+    if (threadIdx.x == 0) *slot_sign(d, out) = sg;
+    __syncthreads();
+}
+
+// G <- exp(+dtau K) exp_v(l)^-1 G exp_v(l) exp(-dtau K)
+__device__ void dqmc_wrap(const ChainDesc& d, Smem& sm, int l) {
+    const int n = d.n, nn = n * n;
+    for (int s = 0; s < 2; ++s) {
+        const int sigma = s ? -1 : 1;
+        load_ev(d, sm.ev, l, sigma);
+        __syncthreads();
+        double* g = sm.g[s];
+        for (int e = threadIdx.x; e < nn; e += kNT) g[e] = (g[e] / sm.ev[e / n]) * sm.ev[e % n];
+        __syncthreads();
+        gemm_left_inplace(g, d.expkinvT, n);
+        __syncthreads();
+        gemm_right_inplace(g, d.expk, n);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// site updates of one time slice (both modes)
+// ---------------------------------------------------------------------------------------
+__device__ void update_slice(const ChainDesc& d, Smem& sm, int l, int sw, uint64_t sweep_id,
+                             int* accepted) {
+    const int n = d.n, nn = n * n, L = d.L;
+    const int step = L - 1 - l;
+    double* g0 = sm.g[0];
+    double* g1 = sm.g[1];
+    int8_t* f = d.field + (size_t)l * n;
+    for (int i = 0; i < n; ++i) {
+        const int pos = step * n + i;
+        const int8_t s_il = f[i];
+        double u;
+        if (d.rng == LQMC_RNG_REPLAY) u = d.uniforms[(size_t)sw * n * L + pos];
+        else u = philox_uniform(d.seed, (uint64_t)d.chain_id, sweep_id, (uint64_t)pos);
+        const double gi0 = g0[i * n + i], gi1 = g1[i * n + i];
+        const double ep = s_il > 0 ? d.c[0] : d.c[1];   // exp(+arg), arg = 2 lambda s
+        const double em = s_il > 0 ? d.c[1] : d.c[0];   // exp(-arg)
+        double ratio, a0, a1;
+        if (d.mode == LQMC_MODE_COMPAT) {
+            const double d_up = __dadd_rn(1.0, __dmul_rn(__dsub_rn(1.0, gi0), __dsub_rn(ep, 1.0)));
+            const double d_dn = __dadd_rn(1.0, __dmul_rn(__dsub_rn(1.0, gi1), __dsub_rn(em, 1.0)));
+            ratio = __dmul_rn(d_up, d_dn);
+            a0 = __dsub_rn(em, 1.0);    // the reference's up-spin update uses exp(-arg) - 1
+            a1 = __dsub_rn(ep, 1.0);
+        } else {
+            const double dl_up = __dsub_rn(ep, 1.0), dl_dn = __dsub_rn(em, 1.0);
+            const double r_up = __dadd_rn(1.0, __dmul_rn(dl_up, __dsub_rn(1.0, gi0)));
+            const double r_dn = __dadd_rn(1.0, __dmul_rn(dl_dn, __dsub_rn(1.0, gi1)));
+            ratio = __dmul_rn(r_up, r_dn);
+            a0 = __ddiv_rn(dl_up, r_up);
+            a1 = __ddiv_rn(dl_dn, r_dn);
+        }
+        const bool acc = (u <= ratio);
+        if (d.record && threadIdx.x == 0)
+            d.decisions[((size_t)sw * L + step) * n + i] = acc ? 1 : 0;
+        if (!acc) continue;
+        const int j = threadIdx.x;
+        if (j < n) {
+            if (d.mode == LQMC_MODE_COMPAT) {
+                // c = -(E-1) G[i,:], c_i += E-1, e = G[:,i] / (1 + c_i)   (lqmc.py:320-327)
+                const double t0 = -a0, t1 = -a1;
+                const double ci0 = __dadd_rn(__dmul_rn(t0, gi0), a0);
+                const double ci1 = __dadd_rn(__dmul_rn(t1, gi1), a1);
+                sm.yv[0][j] = (j == i) ? ci0 : __dmul_rn(t0, g0[i * n + j]);
+                sm.yv[1][j] = (j == i) ? ci1 : __dmul_rn(t1, g1[i * n + j]);
+                sm.xv[0][j] = __ddiv_rn(g0[j * n + i], __dadd_rn(1.0, ci0));
+                sm.xv[1][j] = __ddiv_rn(g1[j * n + i], __dadd_rn(1.0, ci1));
+            } else {
+                // x = G[:,i], y = (Delta/R) (e_i - G[i,:])
+                sm.xv[0][j] = g0[j * n + i];
+                sm.xv[1][j] = g1[j * n + i];
+                sm.yv[0][j] = __dmul_rn((j == i) ? __dadd_rn(-gi0, 1.0) : -g0[i * n + j], a0);
+                sm.yv[1][j] = __dmul_rn((j == i) ? __dadd_rn(-gi1, 1.0) : -g1[i * n + j], a1);
+            }
+        }
+        __syncthreads();
+        if (d.mode == LQMC_MODE_COMPAT) {
+            for (int e = threadIdx.x; e < nn; e += kNT) {
+                const int r = e / n, c = e % n;
+                g0[e] = __dsub_rn(g0[e], __dmul_rn(sm.xv[0][r], sm.yv[0][c]));
+                g1[e] = __dsub_rn(g1[e], __dmul_rn(sm.xv[1][r], sm.yv[1][c]));
+            }
+        } else {
+            for (int e = threadIdx.x; e < nn; e += kNT) {
+                const int r = e / n, c = e % n;
+                g0[e] = fma(-sm.xv[0][r], sm.yv[0][c], g0[e]);
+                g1[e] = fma(-sm.xv[1][r], sm.yv[1][c], g1[e]);
+            }
+        }
+        if (threadIdx.x == 0) {
+            f[i] = (int8_t)(-s_il);
+            ++*accepted;
+        }
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// K7: measurements (lqmc.py:367-375 sums G; Wick observables on top)
+// ---------------------------------------------------------------------------------------
+__device__ void measure(const ChainDesc& d, Smem& sm) {
+    const int n = d.n, nn = n * n;
+    const double* g0 = sm.g[0];
+    const double* g1 = sm.g[1];
+    double* obs = d.obs;
+    for (int e = threadIdx.x; e < nn; e += kNT) {
+        d.gsum[e] += g0[e];
+        d.gsum[nn + e] += g1[e];
+    }
+    double* nu = sm.xv[0];
+    double* nd = sm.xv[1];
+    for (int i = threadIdx.x; i < n; i += kNT) {
+        const double a = 1.0 - g0[i * n + i], b = 1.0 - g1[i * n + i];
+        nu[i] = a;
+        nd[i] = b;
+        obs[LQMC_OBS_HEADER + i] += a + b;
+        obs[LQMC_OBS_HEADER + n + i] += a * b;
+    }
+    __syncthreads();
+    double ek = 0.0, ep = 0.0, dc = 0.0, dn = 0.0;
+    for (int e = threadIdx.x; e < nn; e += kNT) {
+        const int j = e / n, k = e % n;
+        const double kv = d.kinetic[e];
+        if (kv != 0.0) {
+            const double del = (j == k) ? 1.0 : 0.0;
+            ek += kv * ((del - g0[k * n + j]) + (del - g1[k * n + j]));
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += kNT) {
+        ep += (nu[i] - 0.5) * (nd[i] - 0.5);
+        dc += nu[i] * nd[i];
+        dn += nu[i] + nd[i];
+    }
+    ek = block_sum(ek, sm.sv);
+    ep = block_sum(ep, sm.sv);
+    dc = block_sum(dc, sm.sv);
+    dn = block_sum(dn, sm.sv);
+    if (threadIdx.x == 0) {
+        obs[0] += 1.0;
+        obs[1] += ek;
+        obs[2] += d.u * ep;
+        obs[3] += dc / n;
+        obs[4] += dn / n;
+    }
+    double* onn = obs + LQMC_OBS_HEADER + 2 * n;
+    double* osz = onn + nn;
+    for (int e = threadIdx.x; e < nn; e += kNT) {
+        const int i = e / n, j = e % n;
+        const double del = (i == j) ? 1.0 : 0.0;
+        const double same = nu[i] * nu[j] + nd[i] * nd[j] + (del - g0[j * n + i]) * g0[e] +
+                            (del - g1[j * n + i]) * g1[e];
+        const double cross = nu[i] * nd[j] + nd[i] * nu[j];
+        onn[e] += same + cross;
+        osz[e] += 0.25 * (same - cross);
+    }
+    __syncthreads();
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kNT, 1)
+sweep_fp64_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_measure) {
+    extern __shared__ __align__(16) double smem[];
+    __shared__ ChainDesc d;
+    __shared__ int accepted;
+    __shared__ int singular;
+    if (threadIdx.x == 0) {
+        d = descs[blockIdx.x];
+        accepted = 0;
+        singular = 0;
+    }
+    __syncthreads();
+    const int n = d.n, nn = n * n;
+    Smem sm;
+    double* p = smem;
+    sm.sv = p; p += kNW + 8;
+    sm.xv[0] = p; p += n;
+    sm.xv[1] = p; p += n;
+    sm.yv[0] = p; p += n;
+    sm.yv[1] = p; p += n;
+    sm.ev = p; p += n;
+    sm.nrm = p; p += n;
+    sm.tau = p; p += n;
+    sm.dv = p; p += n;
+    sm.order = reinterpret_cast<int*>(p); p += n;
+    p = smem + (((p - smem) + 3) & ~(ptrdiff_t)3);   // 32-byte multiple from the base
+    double* gw = d.work + (size_t)(2 * d.n_chunks + 4) * d.slot;   // spill area after the slots
+    if (d.flags & kGreenInGlobal) { sm.g[0] = gw; sm.g[1] = gw + nn; gw += 2 * nn; }
+    else { sm.g[0] = p; sm.g[1] = p + nn; p += 2 * nn; }
+    if (d.flags & kScratchInGlobal) { sm.s0 = gw; sm.s1 = gw + nn; }
+    else { sm.s0 = p; sm.s1 = p + nn; }
+
+    double max_resid = 0.0;
+    double logdet[2] = {0.0, 0.0}, sgn[2] = {1.0, 1.0};
+    uint64_t sweep_id = (uint64_t)d.diag[7];
+    for (int sw = 0; sw < n_sweeps; ++sw, ++sweep_id) {
+        if (d.mode == LQMC_MODE_COMPAT) {
+            compat_recompute(d, sm, 0, &singular);
+            compat_recompute(d, sm, 1, &singular);
+            for (int l = d.L - 1; l >= 0; --l) {
+                update_slice(d, sm, l, sw, sweep_id, &accepted);
+                __syncthreads();
+                if (l > 0) compat_wrap(d, sm, l - 1);
+            }
+        } else {
+            dqmc_right_stack(d, sm, 0, &logdet[0], &sgn[0], &singular);
+            dqmc_right_stack(d, sm, 1, &logdet[1], &sgn[1], &singular);
+            int lp[2] = {0, 0};
+            for (int c = d.n_chunks - 1; c >= 0; --c) {
+                const int lo = c * d.stab_every;
+                const int hi = min(lo + d.stab_every, d.L);
+                for (int l = hi - 1; l >= lo; --l) {
+                    update_slice(d, sm, l, sw, sweep_id, &accepted);
+                    __syncthreads();
+                    if (l > 0) dqmc_wrap(d, sm, l);
+                }
+                if (c > 0) {
+                    for (int s = 0; s < 2; ++s) {
+                        const bool first = (c == d.n_chunks - 1);
+                        dqmc_left_step(d, sm, s, lp[s], first, lo, hi);
+                        lp[s] ^= 1;
+                        const int rs = right_slot(d, s, c - 1), ls = left_slot(d, s, lp[s]);
+                        const double r = green_udt(d, sm, slot_u(d, rs), slot_d(d, rs), slot_t(d, rs),
+                                                   *slot_sign(d, rs), slot_u(d, ls), slot_d(d, ls),
+                                                   slot_t(d, ls), *slot_sign(d, ls), sm.g[s], true,
+                                                   &logdet[s], &sgn[s], &singular);
+                        max_resid = fmax(max_resid, r);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (do_measure) measure(d, sm);
+        // health check of G (NaN/Inf)
+        int bad = 0;
+        for (int e = threadIdx.x; e < 2 * nn; e += kNT) {
+            const double v = (e < nn) ? sm.g[0][e] : sm.g[1][e - nn];
+            if (!isfinite(v)) bad = 1;
+        }
+        bad = __syncthreads_or(bad);
+        if (bad && threadIdx.x == 0) atomicOr(d.status, LQMC_STATUS_NONFINITE);
+    }
+    for (int e = threadIdx.x; e < nn; e += kNT) {
+        d.green[e] = sm.g[0][e];
+        d.green[nn + e] = sm.g[1][e];
+    }
+    if (threadIdx.x == 0) {
+        d.diag[0] += (double)accepted;
+        d.diag[1] += (double)n_sweeps * n * d.L;
+        d.diag[2] = max_resid;
+        d.diag[3] = logdet[0];
+        d.diag[4] = logdet[1];
+        d.diag[5] = sgn[0];
+        d.diag[6] = sgn[1];
+        d.diag[7] += (double)n_sweeps;
+        if (singular) atomicOr(d.status, LQMC_STATUS_SINGULAR);
+        if (max_resid > d.drift_tol) atomicOr(d.status, LQMC_STATUS_DRIFT);
+    }
+}
+
+// bytes of dynamic shared memory the kernel needs for a chain of n sites with `flags`
+size_t sweep_fp64_smem_bytes(int n, int flags) {
+    size_t v = (size_t)(kNW + 8 + 9 * n);
+    v = ((v + 3) & ~(size_t)3) * sizeof(double);
+    if (!(flags & kGreenInGlobal)) v += 2 * (size_t)n * n * sizeof(double);
+    if (!(flags & kScratchInGlobal)) v += 2 * (size_t)n * n * sizeof(double);
+    return v;
+}
+
+cudaError_t launch_sweep_fp64(const ChainDesc* d_descs, int n_chains, size_t smem, int n_sweeps,
+                              int measure, cudaStream_t stream) {
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(sweep_fp64_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    sweep_fp64_kernel<<<n_chains, kNT, smem, stream>>>(d_descs, n_sweeps, measure);
+    return cudaGetLastError();
+}
+
+}  // namespace lqmc

@@ -1,0 +1,193 @@
+"""Batched Markov-chain engine over liblqmc_gpu.so.
+
+One ``Engine`` holds any number of independent chains (uneven lattice sizes, temperatures
+and interactions allowed) and sweeps them all in one launch per shared-memory footprint.
+It replaces the reference's walker pool (lqmc/multiprocessing.py:252-341), which ran one
+chain per forked process.
+
+Host-side set-up follows ``LatticeQMC.set_beta`` (lqmc/lqmc.py:93-117) with the same numpy /
+scipy call forms, so the float64 constants handed to the device are bit-identical to the
+ones the reference computes:
+    dtau = beta / L;  lambda = arccosh(exp(U dtau / 2)) (0 if U == 0);  exp_k = expm(-dtau K)
+"""
+import ctypes
+
+import numpy as np
+from scipy.linalg import expm
+
+from . import _native
+from ._native import as_f64, ptr
+
+
+def hs_coupling(u, dtau):
+    """lambda = arccosh(exp(U dtau / 2)), or 0 for U == 0 (lqmc/lqmc.py:105)."""
+    return np.arccosh(np.exp(u * dtau / 2.)) if u else 0
+
+
+def exp_constants(lamb, n_sites):
+    """[exp(2 lam), exp(-2 lam), exp(-lam), exp(lam)] in the reference's call forms.
+
+    exp(+-2 lam) are numpy scalar exps of arg = 2 * lamb * s (lqmc/lqmc.py:313-323);
+    exp(-+lam) come from numpy's array exp over an int8 field column (lqmc/lqmc.py:149-154).
+    """
+    e2p = np.exp(+(2 * lamb * np.int8(1)))
+    e2m = np.exp(+(2 * lamb * np.int8(-1)))
+    col = np.array(([1, -1] * ((n_sites + 2) // 2))[:max(n_sites, 2)], dtype=np.int8)
+    ev = np.exp(-1 * 1 * lamb * col)
+    return np.array([e2p, e2m, ev[0], ev[1]], dtype=np.float64)
+
+
+class ChainSpec:
+    """One chain: kinetic matrix K (N, N), interaction u, inverse temperature beta,
+    time slices L and the initial HS field (N, L) int8.
+
+    exp_k, exp_k_inv and consts may be given precomputed (e.g. values recorded on another
+    machine); otherwise they are computed here as the reference does."""
+
+    def __init__(self, kinetic, u, beta, time_steps, field, exp_k=None, exp_k_inv=None,
+                 consts=None):
+        self.kinetic = as_f64(kinetic)
+        self.n = self.kinetic.shape[0]
+        self.u = float(u)
+        self.beta = float(beta)
+        self.L = int(time_steps)
+        self.field = np.ascontiguousarray(field, dtype=np.int8)
+        if self.field.shape != (self.n, self.L):
+            raise ValueError(f"field shape {self.field.shape} != ({self.n}, {self.L})")
+        self.dtau = self.beta / self.L
+        self.lamb = hs_coupling(u, self.dtau)
+        self.exp_k = as_f64(exp_k) if exp_k is not None else expm(-1 * self.dtau * self.kinetic)
+        self.exp_k_inv = None if exp_k_inv is None else as_f64(exp_k_inv)
+        self.consts = None if consts is None else as_f64(consts)
+
+
+class Engine:
+    """Batched DQMC sweep engine on one GPU.
+
+    mode       'compat' (reference arithmetic, lqmc/lqmc.py:301-347) or 'dqmc' (textbook,
+               stabilised)
+    precision  'fp64'
+    rng        'replay' (uniforms uploaded per sweep) or 'philox' (on device)
+    """
+
+    def __init__(self, chains, mode="dqmc", precision="fp64", rng="philox", stab_every=10,
+                 delay=0, seed=0, record=False, device=0):
+        self.chains = list(chains)
+        self.mode, self.precision, self.rng = mode, precision, rng
+        self.record = bool(record)
+        self._h = _native.Handle(mode, precision, rng, stab_every, delay, seed, record, device)
+        n = len(self.chains)
+        n_sites = np.array([c.n for c in self.chains], dtype=np.int32)
+        n_slices = np.array([c.L for c in self.chains], dtype=np.int32)
+        eks, ekis, kins = [], [], []
+        consts = np.zeros((n, 4))
+        us = np.zeros(n)
+        for i, c in enumerate(self.chains):
+            eks.append(as_f64(c.exp_k))
+            if c.exp_k_inv is not None:
+                ekis.append(c.exp_k_inv)
+            elif mode == "compat":
+                ekis.append(as_f64(np.linalg.inv(c.exp_k)))
+            else:
+                ekis.append(as_f64(expm(c.dtau * c.kinetic)))
+            kins.append(c.kinetic)
+            consts[i] = c.consts if c.consts is not None else exp_constants(c.lamb, c.n)
+            us[i] = c.u
+        self._keep = (eks, ekis, kins)
+        arr = ctypes.c_void_p * n
+        p_ek = arr(*[m.ctypes.data for m in eks])
+        p_eki = arr(*[m.ctypes.data for m in ekis])
+        p_kin = arr(*[m.ctypes.data for m in kins])
+        self._h.call("lqmc_set_chains", n, ptr(n_sites), ptr(n_slices), p_ek, p_eki, p_kin,
+                     ptr(consts), ptr(us))
+        for i, c in enumerate(self.chains):
+            self.set_field(i, c.field)
+        self.last_sweeps = 0
+
+    # -- state ---------------------------------------------------------------------------
+    def set_field(self, chain, field):
+        f = np.ascontiguousarray(field, dtype=np.int8)
+        self._h.call("lqmc_set_field", int(chain), ptr(f))
+
+    def field(self, chain):
+        c = self.chains[chain]
+        out = np.empty((c.n, c.L), dtype=np.int8)
+        self._h.call("lqmc_get_field", int(chain), ptr(out))
+        return out
+
+    def set_uniforms(self, chain, uniforms):
+        u = as_f64(uniforms)
+        self._h.call("lqmc_set_uniforms", int(chain), ptr(u), u.size)
+
+    # -- sweeps --------------------------------------------------------------------------
+    def sweep(self, n_sweeps=1, measure=False, stream=None):
+        """Run n_sweeps sweeps of every chain (asynchronous on `stream`, an int handle)."""
+        self._h.call("lqmc_sweep", int(n_sweeps), int(bool(measure)),
+                     ctypes.c_void_p(stream or 0))
+        self.last_sweeps = int(n_sweeps)
+
+    # -- results -------------------------------------------------------------------------
+    def green(self, chain):
+        c = self.chains[chain]
+        out = np.empty((2, c.n, c.n))
+        self._h.call("lqmc_get_green", int(chain), ptr(out))
+        return out
+
+    def green_sum(self, chain):
+        c = self.chains[chain]
+        out = np.empty((2, c.n, c.n))
+        cnt = np.zeros(1, dtype=np.int64)
+        self._h.call("lqmc_get_green_sum", int(chain), ptr(out), ptr(cnt))
+        return out, int(cnt[0])
+
+    def observables_raw(self, chain):
+        c = self.chains[chain]
+        out = np.empty(_native.obs_len(c.n))
+        self._h.call("lqmc_get_observables", int(chain), ptr(out))
+        return out
+
+    def observables(self, chain):
+        """Means over the measured sweeps of chain `chain` (dict)."""
+        n = self.chains[chain].n
+        o = self.observables_raw(chain)
+        cnt = max(o[0], 1.0)
+        h = _native.OBS_HEADER
+        return {
+            "count": int(o[0]),
+            "kinetic_energy": o[1] / cnt,
+            "potential_energy": o[2] / cnt,
+            "double_occupancy_mean": o[3] / cnt,
+            "density_mean": o[4] / cnt,
+            "density": o[h:h + n] / cnt,
+            "double_occupancy": o[h + n:h + 2 * n] / cnt,
+            "nn": o[h + 2 * n:h + 2 * n + n * n].reshape(n, n) / cnt,
+            "szsz": o[h + 2 * n + n * n:h + 2 * n + 2 * n * n].reshape(n, n) / cnt,
+        }
+
+    def reset_measurements(self):
+        self._h.call("lqmc_reset_measurements")
+
+    def decisions(self, chain):
+        c = self.chains[chain]
+        out = np.empty((self.last_sweeps, c.L, c.n), dtype=np.int8)
+        self._h.call("lqmc_get_decisions", int(chain), ptr(out), out.size)
+        return out
+
+    def diagnostics(self, chain):
+        d = np.empty(_native.DIAG_LEN)
+        self._h.call("lqmc_get_diagnostics", int(chain), ptr(d))
+        return {"accepted": d[0], "attempted": d[1], "max_residual": d[2],
+                "logdet": d[3:5].copy(), "sign": d[5:7].copy(), "sweeps": int(d[7])}
+
+    def status(self):
+        s = np.empty(len(self.chains), dtype=np.int32)
+        self._h.check(self._h.lib.lqmc_get_status(self._h.h, ptr(s)))
+        return s
+
+    def launch_count(self):
+        v = np.zeros(1, dtype=np.int64)
+        self._h.check(self._h.lib.lqmc_get_launch_count(self._h.h, ptr(v)))
+        return int(v[0])
+
+    def close(self):
+        self._h.close()

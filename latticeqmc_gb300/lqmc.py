@@ -1,0 +1,140 @@
+"""GPU-backed drop-in for ``lqmc.LatticeQMC`` (lqmc/lqmc.py:14-408).
+
+Same constructor, attributes and loop methods as the reference solver; the sweep itself
+(``_update_step``) runs on the GPU through liblqmc_gpu.so.  Extra keyword arguments choose
+the engine:
+
+mode        'compat' (default): the reference's fast-sweep arithmetic, defects included;
+            fed the reference's field and uniform stream its accept/reject decisions are
+            the reference's.  'dqmc': textbook, QR-stabilised DQMC.
+rng         'replay' (default): one ``np.random.rand()`` per site from numpy's global
+            generator, in sweep order, exactly as lqmc.py:317 draws them.  'philox': on device.
+stab_every  slices between from-scratch refreshes of G (dqmc).
+precision   'fp64'.
+
+``det_mode=True`` runs the exact-ratio chain (mode 'dqmc'): its ratios equal the reference's
+determinant ratios (lqmc.py:244-248) to rounding.
+"""
+import logging
+import time
+
+import numpy as np
+
+from .configuration import Configuration
+from .engine import ChainSpec, Engine, hs_coupling
+
+DEBUG = logging.DEBUG
+_log = logging.getLogger("latticeqmc_gb300")
+
+# largest uniform block uploaded at once in replay mode (doubles)
+_REPLAY_BLOCK = 1 << 24
+
+
+class LatticeQMC:
+
+    def __init__(self, model, beta, time_steps, warmup=300, sweeps=2000, det_mode=False,
+                 log_lvl=DEBUG, *, mode=None, precision="fp64", rng=None, stab_every=10,
+                 seed=0, device=0):
+        self.logger = _log if log_lvl is not None else None
+        if self.logger is not None:
+            self.logger.setLevel(log_lvl)
+        self.model = model
+        self.n_sites = model.n_sites
+        self.time_steps = time_steps
+        self.config = Configuration(self.n_sites, time_steps)
+        self.warm_sweeps = warmup
+        self.meas_sweeps = sweeps
+        self.det_mode = det_mode
+        self.mode = mode or ("dqmc" if det_mode else "compat")
+        self.precision = precision
+        self.rng = rng or "replay"
+        self.stab_every = stab_every
+        self.seed = seed
+        self.device = device
+        self.status = ""
+        self.it = 0
+        self.ratio = 0.0
+        self.acc = False
+        self.ham_kin = self.model.ham_kinetic()
+        self.beta = 0.
+        self.dtau = 0.
+        self.lamb = 0.
+        self.exp_k = None
+        self._engine = None
+        self._log_info(f"Warmup=     {self.warm_sweeps}")
+        self._log_info(f"Measurement={self.meas_sweeps}")
+        self.set_beta(beta)
+
+    def _log_info(self, msg):
+        if self.logger is not None:
+            self.logger.info(msg)
+
+    def set_beta(self, beta):
+        """dtau, lambda and exp_k as lqmc.py:93-117; the device chain is (re)built lazily."""
+        self.dtau = beta / self.time_steps
+        self.beta = beta
+        self.lamb = hs_coupling(self.model.u, self.dtau)
+        self._engine = None
+        spec = ChainSpec(self.ham_kin, self.model.u, beta, self.time_steps, self.config.config)
+        self.exp_k = spec.exp_k
+        self._spec = spec
+
+    def set_temperature(self, temp):
+        self.set_beta(1 / temp)
+
+    @property
+    def engine(self):
+        if self._engine is None:
+            self._engine = Engine([self._spec], mode=self.mode, precision=self.precision,
+                                  rng=self.rng, stab_every=self.stab_every, seed=self.seed,
+                                  device=self.device)
+        return self._engine
+
+    # -- sweeps ----------------------------------------------------------------------------
+    def _run(self, n_sweeps, measure):
+        eng = self.engine
+        eng.set_field(0, self.config.config)
+        per = self.n_sites * self.time_steps
+        done = 0
+        while done < n_sweeps:
+            k = n_sweeps - done
+            if self.rng == "replay":
+                k = max(1, min(k, _REPLAY_BLOCK // per))
+                eng.set_uniforms(0, np.random.rand(k * per))
+            eng.sweep(k, measure=measure)
+            done += k
+        self.config.config = eng.field(0)
+
+    def _update_step(self):
+        """One sweep (lqmc.py:301-347); returns (G_up, G_dn) after slice 0."""
+        self._run(1, False)
+        g = self.engine.green(0)
+        return g[0], g[1]
+
+    def warmup_loop(self):
+        self.status = "Warmup"
+        self._run(self.warm_sweeps, False)
+
+    def measure_loop(self):
+        """Mean of the end-of-sweep G over the measurement sweeps (lqmc.py:356-375)."""
+        self.status = "Measurement"
+        self.engine.reset_measurements()
+        self._run(self.meas_sweeps, True)
+        gsum, cnt = self.engine.green_sum(0)
+        return gsum / max(cnt, 1)
+
+    def observables(self):
+        """Wick observables averaged over the last measurement loop."""
+        return self.engine.observables(0)
+
+    def run_lqmc(self):
+        self.warmup_loop()
+        return self.measure_loop()
+
+    def run(self):
+        t0 = time.time()
+        gf_tau = self.run_lqmc()
+        t = time.time() - t0
+        mins, secs = divmod(t, 60)
+        self._log_info(f"Total time: {int(mins):0>2}:{int(secs):0>2} min")
+        return gf_tau

@@ -1,0 +1,136 @@
+"""Host-side logic (CPU only): lattice/K builder, configuration, constants, tools, C ABI."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden, kinetic_from_golden
+from latticeqmc_gb300 import Configuration, HubbardModel, Lattice
+from latticeqmc_gb300 import _native, tools
+from latticeqmc_gb300.engine import ChainSpec, exp_constants, hs_coupling
+from latticeqmc_gb300 import _split_sweeps
+
+
+@pytest.mark.parametrize("side", [2, 3, 4, 5, 7, 8, 9, 10, 12])
+def test_kinetic_matches_reference(side):
+    m = HubbardModel(u=4, t=1, mu=0)
+    m.build_square(side)
+    np.testing.assert_array_equal(m.ham_kinetic(), kinetic_from_golden(side))
+
+
+def test_kinetic_other_shapes_match_reference():
+    f = golden("kinetic_square.npz")
+    m = HubbardModel(u=4, t=1)
+    m.build_square(3)
+    np.testing.assert_array_equal(m.ham_kinetic(), f["s3_mudefault"])
+    m = HubbardModel(u=4, t=1, mu=0)
+    m.build(6, 1, 0)
+    np.testing.assert_array_equal(m.ham_kinetic(), f["chain6"])
+    m.build(4, 3, (0, 1))
+    np.testing.assert_array_equal(m.ham_kinetic(), f["rect4x3"])
+    m.build(4, 4, None)
+    np.testing.assert_array_equal(m.ham_kinetic(), f["open4x4"])
+
+
+@pytest.mark.parametrize("side", [6, 11, 16, 32])
+def test_periodic_sizes_the_reference_cannot_build(side):
+    """lqmc/lattice.py:1030-1031 raises for these sizes; here every site has 4 neighbours."""
+    m = HubbardModel(u=4, t=1, mu=0)
+    m.build_square(side)
+    k = m.ham_kinetic()
+    assert np.array_equal(k, k.T)
+    assert set(np.sum(k != 0, axis=1)) == {4}
+    # translation invariance: site (x, y) bonds to (x+-1, y), (x, y+-1) modulo side
+    for x, y in ((0, 0), (side - 1, side - 1), (side // 2, 1)):
+        i = x * side + y
+        nbs = {((x + 1) % side) * side + y, ((x - 1) % side) * side + y,
+               x * side + (y + 1) % side, x * side + (y - 1) % side}
+        assert set(np.nonzero(k[i])[0]) == nbs
+
+
+def test_lattice_errors():
+    with pytest.raises(ValueError):
+        Lattice.square().set_periodic_boundary(0)
+    with pytest.raises(ValueError):
+        Lattice.square((0, 3))
+
+
+def test_configuration_draws_like_reference():
+    np.random.seed(4)
+    c = Configuration(5, 7)
+    np.random.seed(4)
+    ref = (2 * np.random.randint(0, 2, size=(5, 7)) - 1).astype(np.int8)
+    np.testing.assert_array_equal(c.config, ref)
+    assert c.config.dtype == np.int8
+    c.update(1, 2)
+    assert c[1, 2] == -ref[1, 2]
+    assert c.copy() == c
+    assert "i\\l" in str(c)
+
+
+def test_engine_constants_match_reference_forms():
+    for name in ("compat_2x2.npz", "compat_4x4.npz", "compat_8x8.npz"):
+        f = golden(name)
+        dtau = float(f["beta"]) / int(f["L"])
+        lamb = hs_coupling(float(f["u"]), dtau)
+        assert lamb == float(f["lamb"])
+        np.testing.assert_array_equal(exp_constants(lamb, f["field0"].shape[0]), f["consts"])
+        spec = ChainSpec(f["kinetic"], float(f["u"]), float(f["beta"]), int(f["L"]), f["field0"])
+        np.testing.assert_array_equal(spec.exp_k, f["exp_k"])
+    assert hs_coupling(0.0, 0.1) == 0
+    np.testing.assert_array_equal(exp_constants(0, 4), np.ones(4))
+
+
+def test_chainspec_validates_field_shape():
+    with pytest.raises(ValueError):
+        ChainSpec(np.zeros((4, 4)), 4.0, 1.0, 10, np.ones((4, 9), np.int8))
+
+
+def test_sweep_split_like_parallel_process_manager():
+    per = _split_sweeps(1001, 8)
+    assert per.sum() == 1001 and per[0] == 125 + 1 and all(per[1:] == 125)
+
+
+def test_tools_match_reference_semantics():
+    g = np.diag([0.25, 0.5, 0.75])
+    np.testing.assert_allclose(tools.filling(g), [0.75, 0.5, 0.25])
+    np.testing.assert_allclose(tools.local_moment(g, g), 2 * np.array([0.75, 0.5, 0.25]) * (1 - np.array([0.75, 0.5, 0.25])))
+    K = kinetic_from_golden(2)
+    tau, gt = tools.compute_pole_gf_tau(K, 2.0)
+    f = golden("u0_known.npz")
+    np.testing.assert_allclose(-gt[..., 0], f["s2_pole_tau0"], atol=1e-14)
+    assert abs(tools.fermi_fct(0.0, 3.0) - 0.5) < 1e-15
+
+
+def _header_symbols():
+    with open(os.path.join(ROOT, "include", "lqmc_gpu.h")) as fh:
+        text = fh.read()
+    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*)\s+(lqmc_\w+)\(", text, re.M)))
+
+
+def test_header_declares_what_binding_binds():
+    assert _header_symbols() == sorted(_native.EXPORTED)
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    if not os.path.exists(_native.LIB_PATH):
+        from latticeqmc_gb300 import build
+        build.build()
+    lib = _native.load()
+    for name in _header_symbols():
+        assert hasattr(lib, name), name
+    assert lib.lqmc_abi_version() == 1
+    # no GPU here: creating a handle must fail with an error code, not crash
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if not has_gpu:
+        import ctypes
+        p = _native.Params()
+        h = ctypes.c_void_p()
+        rc = lib.lqmc_create(ctypes.byref(p), ctypes.byref(h))
+        assert rc in (-1, -2)
+        assert lib.lqmc_last_error(None)

@@ -1,0 +1,157 @@
+"""Pin the CPU oracle against the reference's recorded outputs and known answers (CPU only)."""
+import itertools
+
+import numpy as np
+import pytest
+from scipy.linalg import expm
+
+from conftest import golden, kinetic_from_golden
+from oracle import compat, dqmc, ed, philox
+
+
+@pytest.mark.parametrize("side,n_sweeps", [(2, None), (4, None), (8, 1)])
+def test_compat_oracle_bit_identical_to_reference(side, n_sweeps):
+    f = golden(f"compat_{side}x{side}.npz")
+    field = f["field0"].copy()
+    N, L = field.shape
+    u = f["uniforms"]
+    for sw in range(n_sweeps or int(f["n_sweeps"])):
+        rec = {}
+        g = compat.update_step(f["exp_k"], field, float(f["lamb"]), u[sw * N * L:(sw + 1) * N * L],
+                               record=rec)
+        np.testing.assert_array_equal(rec["accept"], f["accept"][sw])
+        np.testing.assert_array_equal(rec["ratio"], f["ratio"][sw])
+        np.testing.assert_array_equal(np.stack(g), f["green"][sw])
+    if n_sweeps is None:
+        np.testing.assert_array_equal(field, f["field_end"])
+
+
+def test_compat_loop_and_outer_rank1_identical():
+    f = golden("compat_2x2.npz")
+    N, L = f["field0"].shape
+    u = f["uniforms"][:N * L]
+    a = compat.update_step(f["exp_k"], f["field0"].copy(), float(f["lamb"]), u, rank1="loop")
+    b = compat.update_step(f["exp_k"], f["field0"].copy(), float(f["lamb"]), u, rank1="outer")
+    np.testing.assert_array_equal(np.stack(a), np.stack(b))
+
+
+def test_compat_run_matches_reference_run():
+    f = golden("run_2x2.npz")
+    g = compat.run(f["exp_k"], f["field0"].copy(), float(f["lamb"]), f["uniforms"],
+                   int(f["warmup"]), int(f["sweeps"]))
+    np.testing.assert_array_equal(g, f["green_mean"])
+
+
+def test_compat_set_beta_and_constants_match_reference():
+    f = golden("compat_4x4.npz")
+    dtau, lamb, exp_k = compat.set_beta(f["kinetic"], float(f["u"]), float(f["beta"]), int(f["L"]))
+    assert lamb == float(f["lamb"])
+    np.testing.assert_array_equal(exp_k, f["exp_k"])
+    np.testing.assert_array_equal(compat.exp_constants(lamb, 16), f["consts"])
+
+
+def test_diag_product_is_exact_scaling():
+    """np.dot(exp_k, diagflat(d)) equals the column scaling exp_k * d bit for bit, which the
+    device uses in place of the dense product (lqmc.py:182, :341)."""
+    f = golden("compat_8x8.npz")
+    ek = f["exp_k"]
+    d = np.exp(-float(f["lamb"]) * f["field0"][:, 3].astype(np.float64))
+    np.testing.assert_array_equal(np.dot(ek, np.diagflat(d)), ek * d[None, :])
+    np.testing.assert_array_equal(np.dot(np.diagflat(d), ek), d[:, None] * ek)
+
+
+@pytest.mark.parametrize("name", ["det_2x2.npz", "det_4x4.npz"])
+def test_dqmc_ratios_equal_reference_determinant_ratios(name):
+    f = golden(name)
+    N, L = f["field0"].shape
+    ch = dqmc.Chain(f["exp_k"], f["exp_k_inv"], float(f["lamb"]), f["field0"], stab_every=5)
+    u = f["uniforms"]
+    for sw in range(int(f["n_sweeps"])):
+        rec = {}
+        ch.sweep(u[sw * N * L:(sw + 1) * N * L], record=rec)
+        np.testing.assert_array_equal(rec["accept"], f["accept"][sw])
+        np.testing.assert_allclose(rec["ratio"], f["ratio"][sw], rtol=1e-9)
+    np.testing.assert_array_equal(ch.field, f["field_end"])
+
+
+def test_dqmc_u0_known_answer():
+    f = golden("u0_known.npz")
+    for side in (2, 4):
+        K, beta, L = f[f"s{side}_kinetic"], float(f[f"s{side}_beta"]), int(f[f"s{side}_L"])
+        dt = beta / L
+        field = np.ones((side * side, L), np.int8)
+        ch = dqmc.Chain(expm(-dt * K), expm(dt * K), 0.0, field, stab_every=5)
+        g = ch.sweep(np.random.default_rng(0).random(side * side * L))
+        assert np.abs(g[0] - f[f"s{side}_pole_tau0"]).max() < 1e-12
+        assert np.abs(g[1] - f[f"s{side}_pole_tau0"]).max() < 1e-12
+
+
+def test_dqmc_stabilisation_residual_small_at_large_beta():
+    K = kinetic_from_golden(8)
+    beta, L, U = 10.0, 100, 4.0
+    dt = beta / L
+    lamb = np.arccosh(np.exp(U * dt / 2))
+    rng = np.random.default_rng(1)
+    field = (2 * rng.integers(0, 2, (64, L)) - 1).astype(np.int8)
+    ch = dqmc.Chain(expm(-dt * K), expm(dt * K), lamb, field, stab_every=5)
+    ch.sweep(rng.random(64 * L))
+    assert ch.max_resid < 1e-8
+
+
+def test_estimator_equals_exact_diagonalisation_by_enumeration():
+    """Sum over all 2^(N L) HS fields of a 2x2, L=3 lattice: the weighted mean of the
+    engine's Green's-function estimator and Wick measurements equals the Trotterised ED."""
+    K = kinetic_from_golden(2)
+    U, beta, L, N = 4.0, 1.0, 3, 4
+    dt = beta / L
+    lamb = np.arccosh(np.exp(U * dt / 2))
+    ek = expm(-dt * K)
+    wsum, gacc, ekin, docc = 0.0, np.zeros((2, N, N)), 0.0, 0.0
+    for bits in itertools.product((1, -1), repeat=N * L):
+        s = np.array(bits, dtype=np.int8).reshape(N, L)
+        ch = dqmc.Chain(ek, expm(dt * K), lamb, s, stab_every=2)
+        gs, w = [], 1.0
+        for sig in (1, -1):
+            stack = ch.right_stack(sig)
+            # G~_0 = (1 + B_0 B_{L-1} ... B_1): wrap the fresh G~_{L-1} down to slice 0
+            g, logdet, sgn = dqmc.green_from_udt(stack[-1], dqmc.identity_udt(N))
+            for l in range(L - 1, 0, -1):
+                g = ch.wrap(l, g, sig)
+            gs.append(g)
+            w *= sgn * np.exp(-logdet)
+        o = dqmc.measure(np.array(gs), K, U)
+        wsum += w
+        gacc += w * np.array(gs)
+        ekin += w * o["kinetic_energy"]
+        docc += w * o["double_occupancy"].mean()
+    ex = ed.observables(K, U, beta, L)
+    assert abs(ekin / wsum - ex["kinetic_energy"]) < 1e-10
+    assert abs(docc / wsum - ex["double_occupancy"].mean()) < 1e-10
+    assert np.abs(gacc / wsum - ex["green"]).max() < 1e-10
+
+
+def test_ed_u0_is_free_fermions():
+    K = kinetic_from_golden(2)
+    beta, L = 2.0, 10
+    ex = ed.observables(K, 0.0, beta, L)
+    exact = np.linalg.inv(np.eye(4) + expm(-beta * K))
+    np.testing.assert_allclose(ex["green"][0], exact, atol=1e-12)
+    np.testing.assert_allclose(ex["density"], 1.0, atol=1e-12)
+
+
+def test_philox_matches_numpy_philox():
+    for ctr, key in (((0, 0, 0, 0), (0, 0)), ((5, 7, 1, 2), (123, 4)),
+                     ((2 ** 64 - 2, 3, 0, 0), (2 ** 63, 17))):
+        bg = np.random.Philox(counter=np.array(ctr, dtype=np.uint64), key=np.array(key, dtype=np.uint64))
+        raw = [int(x) for x in bg.random_raw(4)]
+        nxt = ((ctr[0] + 1) % 2 ** 64, ctr[1] + (ctr[0] + 1) // 2 ** 64, ctr[2], ctr[3])
+        assert raw == philox.philox4x64(nxt, key)
+
+
+def test_philox_uniforms_in_unit_interval_and_distinct_streams():
+    a = philox.uniforms(1, 0, 0, 16, 20)
+    b = philox.uniforms(1, 1, 0, 16, 20)
+    c = philox.uniforms(1, 0, 1, 16, 20)
+    assert a.min() >= 0.0 and a.max() < 1.0
+    assert not np.array_equal(a, b) and not np.array_equal(a, c)
+    assert abs(np.concatenate([a, b, c]).mean() - 0.5) < 0.05
