@@ -1,0 +1,385 @@
+"""Throughput benchmark of the DQMC sweep engine on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload batched_fp64]
+
+A step is one sweep of every chain of the workload (one lqmc_sweep(1) call).  The metric
+is site-updates/s: sum over chains of N_c * L_c site-update attempts per sweep, divided by
+the time per sweep; sweeps/s is reported beside it.
+
+Workload batched_fp64 (the reference's batched-chains configuration): 512 independent
+chains, 128 each of 4x4, 6x6, 8x8 and 10x10 periodic square lattices, t=1, mu=0, U drawn
+per chain from {2, 4, 6}, beta=4, dtau=0.1 (L=40), textbook DQMC in float64, QR/UDV
+stabilisation every 5 slices, on-device Philox uniforms, HS fields from seeds 0..511.
+Inputs are synthetic (random HS fields), as the reference's own runs are.
+
+value      device throughput with all state resident in HBM.
+e2e        the same sweeps through the public C ABI in replay mode (the drop-in path of
+           LatticeQMC._update_step): each step uploads that sweep's uniforms from pinned
+           host memory and downloads every chain's G, copies inside the timed region.
+roofline   the sweep kernel against the measured float64 throughput of this GPU (cuBLAS
+           DGEMM, timed here); algorithmic flops per sweep and chain
+           8 L N^3 (wraps) + 4 L N^3 (B-chain) + 2 (L / n_s) (4/3) N^3 (QR) + 4 A N^2
+           (A = accepted flips, counted on the device).
+cpu_baseline  the reference's fast sweep restated in Python/numpy (oracle/compat.py, with
+           the pure-Python rank-1 loop of lqmc.py:328-331) on a bounded sample of every
+           lattice size of the workload, one process per host core.
+"""
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "site-updates/s (sweeps/s beside it), DQMC sweep of batched Markov chains"
+UNIT = "site-updates/s"
+
+
+# ----------------------------------------------------------------------------------------
+# workload
+# ----------------------------------------------------------------------------------------
+def workload_batched(rank=0, per_side=128):
+    from latticeqmc_gb300 import ChainSpec, HubbardModel
+    sides = [4, 6, 8, 10]
+    beta, L = 4.0, 40
+    rng = np.random.default_rng(1000 + rank)
+    specs = []
+    kin = {}
+    for side in sides:
+        m = HubbardModel(u=4, t=1, mu=0)
+        m.build_square(side)
+        kin[side] = m.ham_kinetic()
+    for side in sides:
+        for _ in range(per_side):
+            u = float(rng.choice([2.0, 4.0, 6.0]))
+            n = side * side
+            field = (2 * rng.integers(0, 2, (n, L)) - 1).astype(np.int8)
+            specs.append(ChainSpec(kin[side], u, beta, L, field))
+    cfg = {"workload": f"batched_fp64: {4 * per_side} chains = {per_side} x {{4x4, 6x6, 8x8, 10x10}} periodic, "
+                       "U in {2,4,6} per chain, mu=0, beta=4, dtau=0.1 (L=40), dqmc fp64, "
+                       "stab every 5, philox",
+           "chains": len(specs), "sides": sides, "beta": beta, "L": L, "stab_every": 5,
+           "precision": "fp64", "mode": "dqmc"}
+    return specs, cfg
+
+
+def algorithmic_flops(specs, accepted, stab_every):
+    tot = 0.0
+    for c in specs:
+        n, L = c.n, c.L
+        tot += 8.0 * L * n ** 3 + 4.0 * L * n ** 3 + 2.0 * math.ceil(L / stab_every) * (4.0 / 3.0) * n ** 3
+    return tot + sum(4.0 * a * c.n ** 2 for a, c in zip(accepted, specs))
+
+
+# ----------------------------------------------------------------------------------------
+# clocks
+# ----------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------------------
+# CPU baseline (the reference's algorithm, oracle port)
+# ----------------------------------------------------------------------------------------
+def _cpu_worker(args):
+    side, L, beta, u, seconds, seed = args
+    sys.path.insert(0, ROOT)
+    from oracle import compat
+    from latticeqmc_gb300 import HubbardModel
+    from latticeqmc_gb300.engine import ChainSpec
+    m = HubbardModel(u=u, t=1, mu=0)
+    m.build_square(side)
+    n = side * side
+    rng = np.random.default_rng(seed)
+    field = (2 * rng.integers(0, 2, (n, L)) - 1).astype(np.int8)
+    spec = ChainSpec(m.ham_kinetic(), u, beta, L, field)
+    uni = rng.random(n * L)
+    # size the sample from a short probe so that it takes about `seconds`
+    probe = compat.time_sites(spec.exp_k, field.copy(), spec.lamb, uni, min(n * L, 2 * n))
+    sample = int(min(n * L, max(2 * n, seconds / max(probe, 1e-9))))
+    return side, compat.time_sites(spec.exp_k, field.copy(), spec.lamb, uni, sample), sample
+
+
+def cpu_baseline(specs, cfg, seconds_per_size=2.5, cores=None):
+    """Site-updates/s of the workload on `cores` host processes, each running a bounded
+    sample of the reference's sweep for every lattice size."""
+    cores = cores or os.cpu_count() or 1
+    sides = cfg["sides"]
+    jobs = []
+    for p in range(cores):
+        for side in sides:
+            jobs.append((side, cfg["L"], cfg["beta"], 4.0, seconds_per_size, 7 + p))
+    ctx = mp.get_context("spawn")
+    # one BLAS thread per process: the children read this when they import numpy
+    saved = {k: os.environ.get(k) for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS")}
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"
+    os.environ["OMP_NUM_THREADS"] = "1"
+    t0 = time.perf_counter()
+    try:
+        with ctx.Pool(cores) as pool:
+            res = pool.map(_cpu_worker, jobs)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    wall = time.perf_counter() - t0
+    t_site = {s: statistics.mean(r[1] for r in res if r[0] == s) for s in sides}
+    samples = {s: sum(r[2] for r in res if r[0] == s) for s in sides}
+    # one batch sweep = every chain's N L site updates; chains spread over the cores
+    serial = sum(c.n * c.L * t_site[int(round(math.sqrt(c.n)))] for c in specs)
+    per_sweep = serial / cores
+    sites = sum(c.n * c.L for c in specs)
+    return {
+        "value": sites / per_sweep,
+        "unit": UNIT,
+        "cores": cores,
+        "kind": "port",
+        "sample": (f"oracle/compat.py fast sweep (pure-Python rank-1 loop, per-site log line), "
+                   f"{', '.join(f'{s}x{s}: {samples[s]} site updates' for s in sides)} over "
+                   f"{cores} processes, {wall:.1f}s wall; extrapolated to one sweep of all "
+                   f"{len(specs)} chains"),
+        "sweep_seconds": per_sweep,
+    }
+
+
+# ----------------------------------------------------------------------------------------
+# GPU measurement
+# ----------------------------------------------------------------------------------------
+def fp64_peak_tflops(torch):
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(5):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        torch.matmul(a, b)
+        e.record()
+        e.synchronize()
+        best = max(best, 2.0 * n ** 3 / (s.elapsed_time(e) * 1e-3) / 1e12)
+    return best
+
+
+def run_ours(args, rank, world):
+    import torch
+    from latticeqmc_gb300 import Engine
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    specs, cfg = workload_batched(rank, args.per_size)
+    stab = cfg["stab_every"]
+    eng = Engine(specs, mode="dqmc", rng="philox", seed=12345 + 1000003 * rank, stab_every=stab,
+                 device=dev)
+    stream = torch.cuda.Stream()
+    sites = sum(c.n * c.L for c in specs)
+    # warm-up
+    for _ in range(args.warmup):
+        eng.sweep(1, stream=stream.cuda_stream)
+    torch.cuda.synchronize()
+    acc0 = [eng.diagnostics(c)["accepted"] for c in range(len(specs))]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        eng.sweep(1, stream=stream.cuda_stream)
+        launches += eng.launch_count()
+    end.record(stream)
+    end.synchronize()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = start.elapsed_time(end) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+        torch.distributed.barrier()
+    acc1 = [eng.diagnostics(c)["accepted"] for c in range(len(specs))]
+    accepted = [(b - a) / args.steps for a, b in zip(acc0, acc1)]
+    resid = max(eng.diagnostics(c)["max_residual"] for c in range(len(specs)))
+    status_bad = int(np.count_nonzero(eng.status()))
+    flops = algorithmic_flops(specs, accepted, stab)
+    eng.close()
+
+    # end to end through the C ABI: replay uniforms in, every chain's G out, per step
+    eng2 = Engine(specs, mode="dqmc", rng="replay", stab_every=stab, device=dev)
+    total_uni = sites
+    total_g = sum(2 * c.n * c.n for c in specs)
+    steps_all = args.warmup + args.steps
+    pin_u = torch.empty(steps_all * total_uni, dtype=torch.float64, pin_memory=True)
+    pin_u.numpy()[:] = np.random.default_rng(rank).random(steps_all * total_uni)
+    pin_g = torch.empty(total_g, dtype=torch.float64, pin_memory=True)
+    u_np, g_np = pin_u.numpy(), pin_g.numpy()
+    for s in range(args.warmup):
+        eng2.set_uniforms_all(u_np[s * total_uni:(s + 1) * total_uni])
+        eng2.sweep(1, stream=stream.cuda_stream)
+        eng2.green_all(g_np)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for s in range(args.warmup, steps_all):
+        eng2.set_uniforms_all(u_np[s * total_uni:(s + 1) * total_uni])
+        eng2.sweep(1, stream=stream.cuda_stream)
+        eng2.green_all(g_np)
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    eng2.close()
+
+    peak = fp64_peak_tflops(torch) if rank == 0 else None
+    return dict(ms=ms, sites=sites, chains=len(specs), flops=flops, launches=launches,
+                clocks=clk, e2e_ms=e2e_ms, h2d=total_uni * 8, d2h=total_g * 8, cfg=cfg,
+                resid=resid, status_bad=status_bad, peak=peak, specs=specs)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="batched_fp64", choices=["batched_fp64"])
+    ap.add_argument("--cpu-seconds", type=float, default=2.5,
+                    help="seconds of CPU sampling per lattice size and process")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--per-size", type=int, default=128,
+                    help="chains per lattice size (128 is the workload; smaller for profiling)")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        specs, cfg = workload_batched(0, args.per_size)
+        vals = []
+        last = None
+        for s in range(args.warmup + args.steps):
+            last = cpu_baseline(specs, cfg, seconds_per_size=min(args.cpu_seconds, 1.0))
+            if s >= args.warmup:
+                vals.append(last["value"])
+        v = statistics.mean(vals)
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": sum(c.n * c.L for c in specs) / v * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "config": cfg,
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"],
+                                 "kind": "port", "sample": last["sample"]},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    r = run_ours(args, rank, world)
+    sites_all = r["sites"] * world
+    value = sites_all / (r["ms"] * 1e-3)
+    e2e = sites_all / (r["e2e_ms"] * 1e-3)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(r["specs"], r["cfg"], seconds_per_size=args.cpu_seconds)
+        cpu.pop("sweep_seconds", None)
+    if rank == 0:
+        achieved = r["flops"] / (r["ms"] * 1e-3) / 1e12
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"],
+            "sweeps_per_s": 1e3 / r["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(r["cfg"], parallelism=f"chains sharded over {world} GPU(s)",
+                           l2="working set (UDT stacks of 512 chains, ~1.6 GB) exceeds the "
+                              "129 MB L2; no flush"),
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
+                    "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"]},
+            "gpu_launches": r["launches"],
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": r["peak"],
+                         "unit": "TFLOP/s", "frac": achieved / r["peak"] if r["peak"] else None,
+                         "traffic": None,
+                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run "
+                                        "(MEASURED_PEAKS.json carries no float64 figure)",
+                         "kernel": "sweep_fp64_kernel (all launch buckets of one sweep)"},
+            "cpu_baseline": cpu,
+            "clocks": r["clocks"],
+            "accuracy": {"max_stabilisation_residual": r["resid"],
+                         "chains_with_status_flags": r["status_bad"]},
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

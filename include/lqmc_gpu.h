@@ -116,6 +116,11 @@ int lqmc_get_field(lqmc_handle* h, int32_t chain, int8_t* field);
  * np.random.rand() draw per site (lqmc/lqmc.py:317). */
 int lqmc_set_uniforms(lqmc_handle* h, int32_t chain, const double* uniforms, size_t count);
 
+/* Replay mode, every chain at once: the concatenation over chains (in chain order) of each
+ * chain's n_sweeps * N * L uniforms, count = n_sweeps * sum(N * L).  One host-to-device copy
+ * for the whole batch; same meaning as lqmc_set_uniforms per chain. */
+int lqmc_set_uniforms_all(lqmc_handle* h, const double* uniforms, size_t count);
+
 /* Run n_sweeps sweeps of every chain (lqmc/lqmc.py:301-347 per sweep; warmup_loop /
  * measure_loop, :349-375).  measure != 0 accumulates G and the Wick observables after
  * every sweep.  Asynchronous on `stream` (a cudaStream_t, NULL = default stream). */
@@ -124,6 +129,10 @@ int lqmc_sweep(lqmc_handle* h, int32_t n_sweeps, int32_t measure, void* stream);
 /* Green's functions after the last sweep, (2, N, N): the value _update_step returns
  * (lqmc/lqmc.py:347). */
 int lqmc_get_green(lqmc_handle* h, int32_t chain, double* green);
+
+/* G of every chain after the last sweep, concatenated in chain order ((2, N, N) each);
+ * one device-to-host copy for the whole batch. */
+int lqmc_get_green_all(lqmc_handle* h, double* green);
 
 /* Accumulated sum of G over measured sweeps, (2, N, N), and the number of measurements;
  * sum / count is what measure_loop returns (lqmc/lqmc.py:356-375). */

@@ -52,8 +52,10 @@ _SIGS = [
     ("lqmc_set_field", ctypes.c_int, [_P, _I32, _P]),
     ("lqmc_get_field", ctypes.c_int, [_P, _I32, _P]),
     ("lqmc_set_uniforms", ctypes.c_int, [_P, _I32, _P, ctypes.c_size_t]),
+    ("lqmc_set_uniforms_all", ctypes.c_int, [_P, _P, ctypes.c_size_t]),
     ("lqmc_sweep", ctypes.c_int, [_P, _I32, _I32, _P]),
     ("lqmc_get_green", ctypes.c_int, [_P, _I32, _P]),
+    ("lqmc_get_green_all", ctypes.c_int, [_P, _P]),
     ("lqmc_get_green_sum", ctypes.c_int, [_P, _I32, _P, _P]),
     ("lqmc_get_observables", ctypes.c_int, [_P, _I32, _P]),
     ("lqmc_reset_measurements", ctypes.c_int, [_P]),

@@ -45,8 +45,14 @@ struct lqmc_handle {
     int n_chains = 0;
     std::vector<ChainDesc> desc;
     std::vector<char> field_set;
-    std::vector<double*> d_uni;
-    std::vector<size_t> uni_cap, uni_count;
+    double* d_uni = nullptr;           // [chain][sweep][n L], chain c at uni_cap * uni_off[c]
+    size_t uni_cap = 0;                // sweeps of uniforms each chain's region holds
+    std::vector<size_t> uni_off;       // prefix sums of n L
+    size_t uni_total = 0;              // sum of n L
+    std::vector<size_t> uni_count;     // uniforms uploaded and not yet consumed, per chain
+    double* d_green = nullptr;         // [chain][2][n][n], contiguous
+    std::vector<size_t> green_off;
+    size_t green_total = 0;
     double* d_f64 = nullptr;
     int8_t* d_i8 = nullptr;
     int32_t* d_status = nullptr;
@@ -85,9 +91,11 @@ void release(lqmc_handle* h) {
         if (b.done) cudaEventDestroy(b.done);
     }
     h->buckets.clear();
-    for (double* u : h->d_uni)
-        if (u) cudaFree(u);
-    h->d_uni.clear();
+    if (h->d_uni) cudaFree(h->d_uni);
+    h->d_uni = nullptr;
+    h->uni_cap = 0;
+    if (h->d_green) cudaFree(h->d_green);
+    h->d_green = nullptr;
     if (h->d_f64) cudaFree(h->d_f64);
     if (h->d_i8) cudaFree(h->d_i8);
     if (h->d_status) cudaFree(h->d_status);
@@ -178,9 +186,17 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
     h->n_chains = n_chains;
     h->desc.assign(n_chains, ChainDesc{});
     h->field_set.assign(n_chains, 0);
-    h->d_uni.assign(n_chains, nullptr);
-    h->uni_cap.assign(n_chains, 0);
     h->uni_count.assign(n_chains, 0);
+    h->uni_off.assign(n_chains, 0);
+    h->green_off.assign(n_chains, 0);
+    h->uni_total = 0;
+    h->green_total = 0;
+    for (int c = 0; c < n_chains; ++c) {
+        h->uni_off[c] = h->uni_total;
+        h->uni_total += (size_t)n_sites[c] * n_slices[c];
+        h->green_off[c] = h->green_total;
+        h->green_total += 2 * (size_t)n_sites[c] * n_sites[c];
+    }
 
     // layout of the float64 arena
     std::vector<size_t> off(n_chains);
@@ -211,7 +227,7 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
         size_t work = (size_t)(2 * d.n_chunks + 4) * d.slot;
         if (flags & lqmc::kGreenInGlobal) work += 2 * nn;
         if (flags & lqmc::kScratchInGlobal) work += 2 * nn;
-        const size_t need = round_up(nn, kAlign) * 5 + round_up(2 * nn, kAlign) * 2 +
+        const size_t need = round_up(nn, kAlign) * 5 + round_up(2 * nn, kAlign) +
                             round_up(LQMC_OBS_LEN(n), kAlign) + round_up(LQMC_DIAG_LEN, kAlign) +
                             round_up(work, kAlign);
         off[c] = total;
@@ -221,11 +237,14 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
     }
     cudaError_t e = cudaMalloc(&h->d_f64, total * sizeof(double));
     if (e != cudaSuccess) { release(h); return fail(h, LQMC_ERR_NOMEM, "device allocation of " + std::to_string(total * 8) + " bytes failed"); }
+    e = cudaMalloc(&h->d_green, h->green_total * sizeof(double));
+    if (e != cudaSuccess) { release(h); return fail(h, LQMC_ERR_NOMEM, "device allocation of G failed"); }
     e = cudaMalloc(&h->d_i8, total_i8);
     if (e != cudaSuccess) { release(h); return fail(h, LQMC_ERR_NOMEM, "device allocation of the fields failed"); }
     e = cudaMalloc(&h->d_status, sizeof(int32_t) * n_chains);
     if (e != cudaSuccess) { release(h); return fail(h, LQMC_ERR_NOMEM, "device allocation of the status words failed"); }
     LQMC_CK(h, cudaMemset(h->d_f64, 0, total * sizeof(double)));
+    LQMC_CK(h, cudaMemset(h->d_green, 0, h->green_total * sizeof(double)));
     LQMC_CK(h, cudaMemset(h->d_i8, 1, total_i8));
     LQMC_CK(h, cudaMemset(h->d_status, 0, sizeof(int32_t) * n_chains));
 
@@ -241,7 +260,7 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
         double* eki = take(nn);
         double* ekit = take(nn);
         double* kin = take(nn);
-        d.green = take(2 * nn);
+        d.green = h->d_green + h->green_off[c];
         d.gsum = take(2 * nn);
         d.obs = take(LQMC_OBS_LEN(n));
         d.diag = take(LQMC_DIAG_LEN);
@@ -317,6 +336,31 @@ int lqmc_get_field(lqmc_handle* h, int32_t chain, int8_t* field) {
     return LQMC_OK;
 }
 
+// Grow (or, with exact = true, resize) the uniform arena to `sweeps` sweeps per chain,
+// keeping every chain's pending uniforms.
+static int ensure_uniform_capacity(lqmc_handle* h, size_t sweeps, bool exact) {
+    if (sweeps <= h->uni_cap && !(exact && sweeps != h->uni_cap)) return LQMC_OK;
+    for (int c = 0; c < h->n_chains; ++c)
+        if ((size_t)h->uni_count[c] > sweeps * h->desc[c].n * h->desc[c].L) sweeps = h->uni_cap;
+    if (sweeps == h->uni_cap) return LQMC_OK;
+    double* fresh = nullptr;
+    cudaError_t e = cudaMalloc(&fresh, std::max<size_t>(1, sweeps * h->uni_total) * sizeof(double));
+    if (e != cudaSuccess) return fail(h, LQMC_ERR_NOMEM, "uniform buffer allocation failed");
+    for (int c = 0; c < h->n_chains; ++c) {
+        if (h->uni_count[c]) {
+            e = cudaMemcpy(fresh + sweeps * h->uni_off[c], h->d_uni + h->uni_cap * h->uni_off[c],
+                           h->uni_count[c] * sizeof(double), cudaMemcpyDeviceToDevice);
+            if (e != cudaSuccess) { cudaFree(fresh); return cuda_fail(h, e, "uniform buffer copy"); }
+        }
+    }
+    if (h->d_uni) cudaFree(h->d_uni);
+    h->d_uni = fresh;
+    h->uni_cap = sweeps;
+    for (int c = 0; c < h->n_chains; ++c) h->desc[c].uniforms = h->d_uni + sweeps * h->uni_off[c];
+    h->descs_dirty = true;
+    return LQMC_OK;
+}
+
 int lqmc_set_uniforms(lqmc_handle* h, int32_t chain, const double* uniforms, size_t count) {
     int rc = check_chain(h, chain);
     if (rc) return rc;
@@ -326,21 +370,29 @@ int lqmc_set_uniforms(lqmc_handle* h, int32_t chain, const double* uniforms, siz
     const size_t per = (size_t)d.n * d.L;
     if (count % per) return fail(h, LQMC_ERR_INVALID, "uniform count must be a multiple of n_sites * n_slices");
     if ((rc = sync_last(h))) return rc;
-    if (count > h->uni_cap[chain]) {
-        if (h->d_uni[chain]) cudaFree(h->d_uni[chain]);
-        h->d_uni[chain] = nullptr;
-        h->uni_cap[chain] = 0;
-        cudaError_t e = cudaMalloc(&h->d_uni[chain], count * sizeof(double));
-        if (e != cudaSuccess) return fail(h, LQMC_ERR_NOMEM, "uniform buffer allocation failed");
-        h->uni_cap[chain] = count;
-        h->descs_dirty = true;
-    }
-    if (count) LQMC_CK(h, cudaMemcpy(h->d_uni[chain], uniforms, count * sizeof(double), cudaMemcpyHostToDevice));
+    h->uni_count[chain] = 0;
+    if ((rc = ensure_uniform_capacity(h, count / per, false))) return rc;
+    if (count)
+        LQMC_CK(h, cudaMemcpy(h->d_uni + h->uni_cap * h->uni_off[chain], uniforms,
+                              count * sizeof(double), cudaMemcpyHostToDevice));
     h->uni_count[chain] = count;
-    if (h->desc[chain].uniforms != h->d_uni[chain]) {
-        h->desc[chain].uniforms = h->d_uni[chain];
-        h->descs_dirty = true;
-    }
+    return LQMC_OK;
+}
+
+int lqmc_set_uniforms_all(lqmc_handle* h, const double* uniforms, size_t count) {
+    if (!h) return LQMC_ERR_INVALID;
+    if (h->n_chains == 0) return fail(h, LQMC_ERR_STATE, "no chains defined (call lqmc_set_chains)");
+    if (h->p.rng != LQMC_RNG_REPLAY) return fail(h, LQMC_ERR_STATE, "uniforms are only uploaded in replay mode");
+    if (!uniforms || count == 0 || count % h->uni_total)
+        return fail(h, LQMC_ERR_INVALID, "uniform count must be a positive multiple of sum(n_sites * n_slices)");
+    int rc = sync_last(h);
+    if (rc) return rc;
+    const size_t sweeps = count / h->uni_total;
+    for (int c = 0; c < h->n_chains; ++c) h->uni_count[c] = 0;
+    if ((rc = ensure_uniform_capacity(h, sweeps, true))) return rc;
+    // the arena layout [chain][sweep][n L] equals the concatenation the caller passes
+    LQMC_CK(h, cudaMemcpy(h->d_uni, uniforms, count * sizeof(double), cudaMemcpyHostToDevice));
+    for (int c = 0; c < h->n_chains; ++c) h->uni_count[c] = sweeps * h->desc[c].n * h->desc[c].L;
     return LQMC_OK;
 }
 
@@ -420,6 +472,16 @@ int lqmc_get_green(lqmc_handle* h, int32_t chain, double* green) {
     if ((rc = sync_last(h))) return rc;
     const ChainDesc& d = h->desc[chain];
     LQMC_CK(h, cudaMemcpy(green, d.green, 2 * (size_t)d.n * d.n * sizeof(double), cudaMemcpyDeviceToHost));
+    return LQMC_OK;
+}
+
+int lqmc_get_green_all(lqmc_handle* h, double* green) {
+    if (!h) return LQMC_ERR_INVALID;
+    if (h->n_chains == 0) return fail(h, LQMC_ERR_STATE, "no chains defined (call lqmc_set_chains)");
+    if (!green) return fail(h, LQMC_ERR_INVALID, "null output");
+    int rc = sync_last(h);
+    if (rc) return rc;
+    LQMC_CK(h, cudaMemcpy(green, h->d_green, h->green_total * sizeof(double), cudaMemcpyDeviceToHost));
     return LQMC_OK;
 }
 

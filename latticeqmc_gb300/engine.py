@@ -119,6 +119,12 @@ class Engine:
         u = as_f64(uniforms)
         self._h.call("lqmc_set_uniforms", int(chain), ptr(u), u.size)
 
+    def set_uniforms_all(self, uniforms):
+        """Uniforms of every chain in one copy: concatenation over chains of
+        (n_sweeps, N*L) blocks.  `uniforms` may be pinned host memory (a numpy view)."""
+        u = as_f64(uniforms)
+        self._h.call("lqmc_set_uniforms_all", ptr(u), u.size)
+
     # -- sweeps --------------------------------------------------------------------------
     def sweep(self, n_sweeps=1, measure=False, stream=None):
         """Run n_sweeps sweeps of every chain (asynchronous on `stream`, an int handle)."""
@@ -131,6 +137,14 @@ class Engine:
         c = self.chains[chain]
         out = np.empty((2, c.n, c.n))
         self._h.call("lqmc_get_green", int(chain), ptr(out))
+        return out
+
+    def green_all(self, out=None):
+        """G of every chain, concatenated (sum of 2 N^2 doubles), in one copy."""
+        total = sum(2 * c.n * c.n for c in self.chains)
+        if out is None:
+            out = np.empty(total)
+        self._h.call("lqmc_get_green_all", ptr(out))
         return out
 
     def green_sum(self, chain):

@@ -57,7 +57,12 @@ def greens_from_scratch(exp_k, field, lamb):
     return gf_up, gf_dn
 
 
-def update_step(exp_k, field, lamb, uniforms, rank1="outer", record=None):
+class _SampleDone(Exception):
+    pass
+
+
+def update_step(exp_k, field, lamb, uniforms, rank1="outer", record=None, max_sites=None,
+                log_line=False):
     """One fast sweep, lqmc.py:301-347.
 
     Parameters
@@ -69,6 +74,10 @@ def update_step(exp_k, field, lamb, uniforms, rank1="outer", record=None):
                                  the reference draws exactly one np.random.rand() per site
     record : dict or None        if given, receives 'accept' (L, N) int8 and 'ratio' (L, N)
                                  indexed [L-1-l_step, i] in sweep order
+    max_sites : int or None      stop after this many site updates and return None (used to
+                                 time a bounded sample of a sweep)
+    log_line : bool              also build the per-site log line the reference formats on
+                                 every site, logger or not (lqmc.py:217-232, :335)
 
     Returns (gf_up, gf_dn) after slice 0 (not wrapped), as lqmc.py:347.
     """
@@ -87,6 +96,8 @@ def update_step(exp_k, field, lamb, uniforms, rank1="outer", record=None):
             pos += 1
             acc_rec[step, i] = acc
             rat_rec[step, i] = ratio
+            if max_sites is not None and pos > max_sites:
+                raise _SampleDone()
             if acc:
                 c_up = -(np.exp(-arg) - 1) * gf_up[i, :]
                 c_up[i] += (np.exp(-arg) - 1)
@@ -104,6 +115,8 @@ def update_step(exp_k, field, lamb, uniforms, rank1="outer", record=None):
                     gf_up = gf_up - e_up[:, None] * c_up[None, :]
                     gf_dn = gf_dn - e_dn[:, None] * c_dn[None, :]
                 field[i, l] *= -1
+            if log_line:
+                _ = f"{l:>2} {i:>2} -- {ratio:.1f} ({acc}) -- {np.mean(field):.3f} {np.var(field):.3f}"
         if l > 0:
             exp_v_up = get_exp_v(field, lamb, l - 1, +1)
             exp_v_dn = get_exp_v(field, lamb, l - 1, -1)
@@ -115,6 +128,21 @@ def update_step(exp_k, field, lamb, uniforms, rank1="outer", record=None):
         record["accept"] = acc_rec
         record["ratio"] = rat_rec
     return gf_up, gf_dn
+
+
+def time_sites(exp_k, field, lamb, uniforms, n_sites_sample):
+    """Seconds per site update of the reference's fast sweep (pure-Python rank-1 loop and
+    per-site log line, as lqmc.py:301-347 runs with log_lvl=None), timed over the first
+    ``n_sites_sample`` site updates of a sweep."""
+    import time
+    t0 = time.perf_counter()
+    try:
+        update_step(exp_k, field, lamb, uniforms, rank1="loop", max_sites=n_sites_sample,
+                    log_line=True)
+        done = field.size
+    except _SampleDone:
+        done = n_sites_sample
+    return (time.perf_counter() - t0) / done
 
 
 def run(exp_k, field, lamb, uniforms, warmup, sweeps):

@@ -38,8 +38,9 @@ def test_error_codes():
         eng.set_field(0, np.zeros((4, 20), np.int8))
     assert e.value.code == -1
     # chain index out of range
-    with pytest.raises(_native.LqmcError):
-        eng.green(1)
+    out = np.zeros((2, 4, 4))
+    assert lib.lqmc_get_green(eng._h.h, 1, _native.ptr(out)) == -1
+    assert lib.lqmc_get_green(eng._h.h, -1, _native.ptr(out)) == -1
     eng.close()
     # lattices above the shared-memory engine's limit in fp64
     with pytest.raises(_native.LqmcError) as e:
