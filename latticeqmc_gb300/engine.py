@@ -37,6 +37,14 @@ def exp_constants(lamb, n_sites):
     return np.array([e2p, e2m, ev[0], ev[1]], dtype=np.float64)
 
 
+def auto_stab_every(chains):
+    """Slices between refreshes of G: the largest n_s with n_s * dtau <= 0.5 for every chain.
+
+    The wraps between refreshes amplify rounding by up to exp(n_s dtau (8t + 2 lambda)); at
+    n_s dtau <= 0.5 the float64 G stays within ~1e-12 of a fresh recompute."""
+    return max(1, min(int(0.5 / c.dtau + 1e-9) for c in chains))
+
+
 class ChainSpec:
     """One chain: kinetic matrix K (N, N), interaction u, inverse temperature beta,
     time slices L and the initial HS field (N, L) int8.
@@ -70,9 +78,12 @@ class Engine:
     rng        'replay' (uniforms uploaded per sweep) or 'philox' (on device)
     """
 
-    def __init__(self, chains, mode="dqmc", precision="fp64", rng="philox", stab_every=10,
+    def __init__(self, chains, mode="dqmc", precision="fp64", rng="philox", stab_every=None,
                  delay=0, seed=0, record=False, device=0):
         self.chains = list(chains)
+        if stab_every is None:
+            stab_every = auto_stab_every(self.chains)
+        self.stab_every = int(stab_every)
         self.mode, self.precision, self.rng = mode, precision, rng
         self.record = bool(record)
         self._h = _native.Handle(mode, precision, rng, stab_every, delay, seed, record, device)

@@ -9,7 +9,8 @@ mode        'compat' (default): the reference's fast-sweep arithmetic, defects i
             the reference's.  'dqmc': textbook, QR-stabilised DQMC.
 rng         'replay' (default): one ``np.random.rand()`` per site from numpy's global
             generator, in sweep order, exactly as lqmc.py:317 draws them.  'philox': on device.
-stab_every  slices between from-scratch refreshes of G (dqmc).
+stab_every  slices between from-scratch refreshes of G (dqmc); default: the largest with
+            stab_every * dtau <= 0.5.
 precision   'fp64'.
 
 ``det_mode=True`` runs the exact-ratio chain (mode 'dqmc'): its ratios equal the reference's
@@ -33,7 +34,7 @@ _REPLAY_BLOCK = 1 << 24
 class LatticeQMC:
 
     def __init__(self, model, beta, time_steps, warmup=300, sweeps=2000, det_mode=False,
-                 log_lvl=DEBUG, *, mode=None, precision="fp64", rng=None, stab_every=10,
+                 log_lvl=DEBUG, *, mode=None, precision="fp64", rng=None, stab_every=None,
                  seed=0, device=0):
         self.logger = _log if log_lvl is not None else None
         if self.logger is not None:
