@@ -167,6 +167,64 @@ void lqmc_destroy(lqmc_handle* h);
 /* LQMC_ABI_VERSION of the loaded library. */
 int lqmc_abi_version(void);
 
+/* ---------------------------------------------------------------------------------------
+ * Allocation-free sweep of one chain.  No counterpart in the reference: it exists for
+ * callers that cannot call cudaMalloc -- applications whose device memory belongs to their
+ * own allocator or arena (a host code that hands this library a fixed set of buffers), and
+ * time-stepping loops that cannot afford the device-wide synchronisation cudaMalloc and
+ * cudaFree may imply.
+ *
+ * The caller passes every input and output as DEVICE pointers it already owns; the scratch
+ * the dqmc sweep needs (the UDT stacks of the stabilised B-chain products and the chain
+ * descriptor) lives in one static device array of LQMC_STATIC_SCRATCH_BYTES (4 MiB) inside
+ * the library, which every GPU that loads the library keeps until the process exits.
+ *
+ * Limits: mode dqmc, precision fp64, 1 <= n_sites <= LQMC_STATIC_MAX_SITES (64),
+ * n_slices >= 1, 1 <= stab_every, and (2 ceil(n_slices / stab_every) + 4) * slot doubles
+ * plus 512 bytes must fit in the array, slot = 2 n^2 + n + 1 rounded up to a multiple of 4
+ * (e.g. n = 64 allows up to 29 chunks, n = 16 up to 490).  Larger sizes are rejected with
+ * LQMC_ERR_INVALID and a message in error_message.
+ *
+ * Every call shares the one array, which keeps the previous call's contents (the sweep
+ * writes every scratch value before reading it, so nothing needs clearing): calls that
+ * overlap on the GPU -- on different streams, or from different host threads -- race and
+ * must be serialised by the caller.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) for that device; make that first call before any
+ * stream capture.  Asynchronous on `stream` (NULL = default stream); results are valid
+ * once the stream has been synchronised.
+ * --------------------------------------------------------------------------------------- */
+#define LQMC_STATIC_SCRATCH_BYTES (4u << 20)
+#define LQMC_STATIC_MAX_SITES 64
+
+typedef struct lqmc_static_chain {
+    int32_t n_sites;
+    int32_t n_slices;
+    int32_t stab_every;
+    int32_t rng;               /* LQMC_RNG_REPLAY (uniforms given) or LQMC_RNG_PHILOX       */
+    uint64_t seed;             /* philox key word 0                                         */
+    int32_t chain_id;          /* philox key word 1                                         */
+    int32_t measure;           /* != 0: accumulate green_sum and obs after every sweep      */
+    double exp_consts[4];      /* exp(2 lambda), exp(-2 lambda), exp(-lambda), exp(lambda)  */
+    double u;                  /* Hubbard U                                                 */
+    const double* exp_k;       /* device, n x n: expm(-dtau K)                              */
+    const double* exp_k_t;     /* device, its transpose                                     */
+    const double* exp_k_inv;   /* device, n x n: expm(+dtau K)                              */
+    const double* exp_k_inv_t; /* device, its transpose                                     */
+    const double* kinetic;     /* device, n x n: K                                          */
+    int8_t* field;             /* device, [n_slices][n_sites], +-1, updated in place        */
+    const double* uniforms;    /* device, replay: n_sweeps * n_sites * n_slices; else NULL  */
+    double* green;             /* device out, (2, n, n): G after the last sweep             */
+    double* green_sum;         /* device in/out, (2, n, n) measurement sum                  */
+    double* obs;               /* device in/out, LQMC_OBS_LEN(n)                            */
+    double* diag;              /* device in/out, LQMC_DIAG_LEN (zero before the first call) */
+    int32_t* status;           /* device in/out, LQMC_STATUS_* bits                         */
+    char* error_message;       /* optional host buffer for a message on failure             */
+    size_t error_capacity;
+} lqmc_static_chain;
+
+/* Run n_sweeps dqmc sweeps of the chain described by *chain without allocating memory. */
+int lqmc_sweep_static(const lqmc_static_chain* chain, int32_t n_sweeps, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -65,6 +65,7 @@ _SIGS = [
     ("lqmc_get_launch_count", ctypes.c_int, [_P, _P]),
     ("lqmc_last_error", ctypes.c_char_p, [_P]),
     ("lqmc_destroy", None, [_P]),
+    ("lqmc_sweep_static", ctypes.c_int, [_P, _I32, _P]),
 ]
 EXPORTED = [s[0] for s in _SIGS]
 

@@ -579,3 +579,114 @@ cudaError_t launch_sweep_fp64(const ChainDesc* d_descs, int n_chains, size_t sme
 }
 
 }  // namespace lqmc
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free single-chain entry point (lqmc_sweep_static, include/lqmc_gpu.h).
+// The chain descriptor and the UDT scratch of the sweep live in one static device array;
+// the unchanged sweep kernel runs on it.
+// ---------------------------------------------------------------------------------------
+#include <cstdio>
+#include <mutex>
+
+namespace {
+
+constexpr size_t kStaticDescBytes = 512;   // ChainDesc slot at the start of the array
+static_assert(sizeof(lqmc::ChainDesc) <= kStaticDescBytes, "descriptor slot too small");
+constexpr int kStaticMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_static_scratch[LQMC_STATIC_SCRATCH_BYTES];
+
+std::mutex g_static_mutex;
+void* g_static_addr[kStaticMaxDevices];   // device address of g_static_scratch, per device
+
+int static_fail(const lqmc_static_chain* c, int code, const char* msg) {
+    if (c && c->error_message && c->error_capacity) {
+        std::snprintf(c->error_message, c->error_capacity, "%s", msg);
+    }
+    return code;
+}
+
+}  // namespace
+
+extern "C" int lqmc_sweep_static(const lqmc_static_chain* c, int32_t n_sweeps, void* stream) {
+    if (!c) return LQMC_ERR_INVALID;
+    if (n_sweeps < 0) return static_fail(c, LQMC_ERR_INVALID, "n_sweeps < 0");
+    const int n = c->n_sites, L = c->n_slices;
+    if (n < 1 || n > LQMC_STATIC_MAX_SITES || L < 1 || c->stab_every < 1)
+        return static_fail(c, LQMC_ERR_INVALID,
+                           "lqmc_sweep_static: needs 1 <= n_sites <= 64, n_slices >= 1, stab_every >= 1");
+    if (c->rng != LQMC_RNG_REPLAY && c->rng != LQMC_RNG_PHILOX)
+        return static_fail(c, LQMC_ERR_INVALID, "lqmc_sweep_static: unknown rng");
+    if (!c->exp_k || !c->exp_k_t || !c->exp_k_inv || !c->exp_k_inv_t || !c->kinetic || !c->field ||
+        !c->green || !c->green_sum || !c->obs || !c->diag || !c->status ||
+        (c->rng == LQMC_RNG_REPLAY && !c->uniforms))
+        return static_fail(c, LQMC_ERR_INVALID, "lqmc_sweep_static: null device pointer");
+    const int stab = c->stab_every < L ? c->stab_every : L;
+    const int chunks = (L + stab - 1) / stab;
+    const size_t slot = ((size_t)2 * n * n + n + 1 + 3) / 4 * 4;
+    const size_t need = kStaticDescBytes + (size_t)(2 * chunks + 4) * slot * sizeof(double);
+    if (need > LQMC_STATIC_SCRATCH_BYTES) {
+        char msg[200];
+        std::snprintf(msg, sizeof(msg),
+                      "lqmc_sweep_static: %zu bytes of scratch needed for n_sites=%d and %d "
+                      "chunks; the static array holds %u", need, n, chunks,
+                      (unsigned)LQMC_STATIC_SCRATCH_BYTES);
+        return static_fail(c, LQMC_ERR_INVALID, msg);
+    }
+    if (n_sweeps == 0) return LQMC_OK;
+
+    // set-up, once per device, with that device current: the array's device address
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return static_fail(c, LQMC_ERR_CUDA, cudaGetErrorString(e));
+    if (dev < 0 || dev >= kStaticMaxDevices) return static_fail(c, LQMC_ERR_CUDA, "device ordinal too large");
+    unsigned char* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_static_mutex);
+        if (!g_static_addr[dev]) {
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_static_scratch);
+            if (e != cudaSuccess || !p) return static_fail(c, LQMC_ERR_CUDA, cudaGetErrorString(e));
+            g_static_addr[dev] = p;
+        }
+        base = static_cast<unsigned char*>(g_static_addr[dev]);
+    }
+
+    lqmc::ChainDesc d{};
+    d.n = n;
+    d.L = L;
+    d.stab_every = stab;
+    d.n_chunks = chunks;
+    d.mode = LQMC_MODE_DQMC;
+    d.rng = c->rng;
+    d.record = 0;
+    d.flags = 0;   // n <= 64: G and both scratch matrices fit in shared memory
+    d.chain_id = c->chain_id;
+    d.slot = (int32_t)slot;
+    d.seed = c->seed;
+    for (int k = 0; k < 4; ++k) d.c[k] = c->exp_consts[k];
+    d.u = c->u;
+    d.drift_tol = 1e-6;
+    d.expk = c->exp_k;
+    d.expkT = c->exp_k_t;
+    d.expkinv = c->exp_k_inv;
+    d.expkinvT = c->exp_k_inv_t;
+    d.kinetic = c->kinetic;
+    d.field = c->field;
+    d.green = c->green;
+    d.gsum = c->green_sum;
+    d.obs = c->obs;
+    d.diag = c->diag;
+    d.work = reinterpret_cast<double*>(base + kStaticDescBytes);
+    d.uniforms = c->uniforms;
+    d.decisions = nullptr;
+    d.status = c->status;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    e = cudaMemcpyAsync(base, &d, sizeof(d), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return static_fail(c, LQMC_ERR_CUDA, cudaGetErrorString(e));
+    e = lqmc::launch_sweep_fp64(reinterpret_cast<const lqmc::ChainDesc*>(base), 1,
+                                lqmc::sweep_fp64_smem_bytes(n, 0), n_sweeps, c->measure ? 1 : 0, st);
+    if (e != cudaSuccess) return static_fail(c, LQMC_ERR_CUDA, cudaGetErrorString(e));
+    return LQMC_OK;
+}
+
