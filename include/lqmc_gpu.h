@@ -73,8 +73,11 @@ extern "C" {
  *   [0] accepted flips (cumulative)  [1] attempted flips (cumulative)
  *   [2] max stabilisation residual max|G_wrapped - G_scratch| of the last launch
  *   [3] log|det G_up|  [4] log|det G_dn|  [5] sign det G_up  [6] sign det G_dn
- *   [7] sweeps done (cumulative; the philox sweep counter)                                */
-#define LQMC_DIAG_LEN 8
+ *   [7] sweeps done (cumulative; the philox sweep counter)
+ *   [8..12] SM clock cycles of the last lqmc_sweep spent per phase (thread 0 of the chain's
+ *   CTA): [8] from-scratch recompute of G, [9] site updates, [10] wraps, [11] stabilisation
+ *   refreshes, [12] measurements.  [13..15] reserved.                                         */
+#define LQMC_DIAG_LEN 16
 
 typedef struct lqmc_params {
     int32_t mode;          /* LQMC_MODE_*                                                  */
@@ -85,8 +88,14 @@ typedef struct lqmc_params {
     int32_t record;        /* 1: keep per-site accept decisions of the last lqmc_sweep    */
     uint64_t seed;         /* Philox key word 0 (LQMC_RNG_PHILOX)                          */
     int32_t device;        /* CUDA device ordinal                                          */
-    int32_t reserved[7];
+    int32_t engine;        /* LQMC_ENGINE_*: which sweep kernel runs the chains            */
+    int32_t reserved[6];
 } lqmc_params;
+
+/* sweep kernels (lqmc_params.engine) */
+#define LQMC_ENGINE_AUTO 0   /* shared-memory kernel for fp64 and n <= 128, else tiled        */
+#define LQMC_ENGINE_SMEM 1   /* one CTA per chain, G in shared memory (fp64, n <= 128)        */
+#define LQMC_ENGINE_TILED 2  /* one CTA per chain, matrices in global memory, tiled GEMMs     */
 
 typedef struct lqmc_handle lqmc_handle;
 

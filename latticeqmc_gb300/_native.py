@@ -18,9 +18,10 @@ ERRORS = {-1: "LQMC_ERR_INVALID", -2: "LQMC_ERR_CUDA", -3: "LQMC_ERR_STATE",
 MODES = {"compat": 0, "dqmc": 1}
 PRECISIONS = {"fp64": 0, "mixed": 1}
 RNGS = {"replay": 0, "philox": 1}
+ENGINES = {"auto": 0, "smem": 1, "tiled": 2}
 STATUS_NONFINITE, STATUS_SINGULAR, STATUS_DRIFT = 1, 2, 4
 OBS_HEADER = 8
-DIAG_LEN = 8
+DIAG_LEN = 16
 
 
 def obs_len(n):
@@ -30,8 +31,8 @@ def obs_len(n):
 class Params(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("precision", ctypes.c_int32), ("rng", ctypes.c_int32),
                 ("stab_every", ctypes.c_int32), ("delay", ctypes.c_int32), ("record", ctypes.c_int32),
-                ("seed", ctypes.c_uint64), ("device", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 7)]
+                ("seed", ctypes.c_uint64), ("device", ctypes.c_int32), ("engine", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 6)]
 
 
 class LqmcError(RuntimeError):
@@ -95,11 +96,12 @@ def ptr(a):
 class Handle:
     """Owns one lqmc_handle; every call checks the return code."""
 
-    def __init__(self, mode, precision, rng, stab_every, delay, seed, record, device):
+    def __init__(self, mode, precision, rng, stab_every, delay, seed, record, device,
+                 engine="auto"):
         self.lib = load()
         p = Params(mode=MODES[mode], precision=PRECISIONS[precision], rng=RNGS[rng],
                    stab_every=int(stab_every), delay=int(delay), record=int(bool(record)),
-                   seed=int(seed) & ((1 << 64) - 1), device=int(device))
+                   seed=int(seed) & ((1 << 64) - 1), device=int(device), engine=ENGINES[engine])
         h = ctypes.c_void_p()
         rc = self.lib.lqmc_create(ctypes.byref(p), ctypes.byref(h))
         if rc != LQMC_OK:

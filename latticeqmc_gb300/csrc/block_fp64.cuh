@@ -62,7 +62,7 @@ __device__ __forceinline__ void set_identity(double* x, int n) {
 }
 
 // X <- A X in place (column-local).  at[m n + j] = A[j][m].
-__device__ void gemm_left_inplace(double* x, const double* __restrict__ at, int n) {
+__device__ inline void gemm_left_inplace(double* x, const double* __restrict__ at, int n) {
     const int lane = lane_id();
     for (int k = warp_id(); k < n; k += kNW) {
         double acc[kMaxRows] = {0.0, 0.0, 0.0, 0.0};
@@ -86,7 +86,7 @@ __device__ void gemm_left_inplace(double* x, const double* __restrict__ at, int 
 }
 
 // X <- X A in place (row-local).  a row-major.
-__device__ void gemm_right_inplace(double* x, const double* __restrict__ a, int n) {
+__device__ inline void gemm_right_inplace(double* x, const double* __restrict__ a, int n) {
     const int lane = lane_id();
     for (int j = warp_id(); j < n; j += kNW) {
         double acc[kMaxRows] = {0.0, 0.0, 0.0, 0.0};
@@ -112,7 +112,7 @@ __device__ void gemm_right_inplace(double* x, const double* __restrict__ a, int 
 
 // C = op(A) op(B), out of place.  TA: A stored transposed (C = A^T B); TB: C = A B^T.
 template <bool TA, bool TB>
-__device__ void gemm(double* __restrict__ c, const double* a, const double* b, int n) {
+__device__ inline void gemm(double* __restrict__ c, const double* a, const double* b, int n) {
     const int lane = lane_id();
     for (int i = warp_id(); i < n; i += kNW) {
         double acc[kMaxRows] = {0.0, 0.0, 0.0, 0.0};
@@ -136,7 +136,7 @@ __device__ void gemm(double* __restrict__ c, const double* a, const double* b, i
 // idamax).  On return rhs holds Z and w its LU factors.  Returns log|det W| through
 // *logabs (thread-uniform) and sign(det W) through *sgn; *singular = 1 on a zero pivot.
 // `sv` is scratch shared memory of at least kNW + 2 doubles.
-__device__ void lu_solve(double* w, double* rhs, int n, double* sv, double* logabs,
+__device__ inline void lu_solve(double* w, double* rhs, int n, double* sv, double* logabs,
                          double* sgn, int* singular) {
     const int lane = lane_id();
     int* spiv = reinterpret_cast<int*>(sv + kNW);
@@ -213,7 +213,7 @@ __device__ void lu_solve(double* w, double* rhs, int n, double* sv, double* loga
 // triangle, reflector vectors v (v_j = 1 implied) below it, tau[j] in `tau` (shared).
 // Returns the number of non-trivial reflectors (det Q = (-1)^count).
 // `sv` is scratch shared memory of at least kNW + 4 doubles.
-__device__ int householder_qr(double* s, double* tau, int n, double* sv) {
+__device__ inline int householder_qr(double* s, double* tau, int n, double* sv) {
     const int lane = lane_id();
     int nrefl = 0;
     for (int j = 0; j < n - 1; ++j) {
@@ -260,7 +260,7 @@ __device__ int householder_qr(double* s, double* tau, int n, double* sv) {
 }
 
 // Q = H_0 H_1 ... H_{n-2} from the reflectors householder_qr left in s / tau.
-__device__ void householder_form_q(double* q, const double* s, const double* tau, int n) {
+__device__ inline void householder_form_q(double* q, const double* s, const double* tau, int n) {
     const int lane = lane_id();
     set_identity(q, n);
     __syncthreads();

@@ -16,18 +16,27 @@ namespace lqmc {
 size_t sweep_fp64_smem_bytes(int n, int flags);
 cudaError_t launch_sweep_fp64(const ChainDesc* d_descs, int n_chains, size_t smem, int n_sweeps,
                               int measure, cudaStream_t stream);
+size_t sweep_tiled_smem_bytes(int n, bool fp32);
+size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32);
+cudaError_t launch_sweep_tiled(const ChainDesc* d_descs, int n_chains, size_t smem, bool fp32,
+                               int n_sweeps, int measure, cudaStream_t stream);
 }  // namespace lqmc
 
 using lqmc::ChainDesc;
 
 namespace {
 
-constexpr int kMaxSitesFp64 = 128;
+constexpr int kMaxSitesSmem = 128;    // one-CTA shared-memory kernel (both modes)
+constexpr int kMaxSitesTiled = 2048;  // tiled kernel (dqmc mode)
+
+// which sweep kernel runs a chain
+enum Kind : int { kSmemFp64 = 0, kTiledFp64 = 1, kTiledFp32 = 2 };
 constexpr size_t kAlign = 32;   // doubles (256 bytes) between device sub-buffers
 
 std::string g_create_error;
 
 struct Bucket {
+    int kind = kSmemFp64;
     size_t smem = 0;
     std::vector<int> chains;
     ChainDesc* d_descs = nullptr;
@@ -137,12 +146,16 @@ int lqmc_create(const lqmc_params* params, lqmc_handle** out) {
         return fail(nullptr, LQMC_ERR_INVALID, "unknown precision");
     if (params->rng != LQMC_RNG_REPLAY && params->rng != LQMC_RNG_PHILOX)
         return fail(nullptr, LQMC_ERR_INVALID, "unknown rng");
+    if (params->engine < LQMC_ENGINE_AUTO || params->engine > LQMC_ENGINE_TILED)
+        return fail(nullptr, LQMC_ERR_INVALID, "unknown engine");
+    if (params->engine == LQMC_ENGINE_SMEM && params->precision == LQMC_PREC_MIXED)
+        return fail(nullptr, LQMC_ERR_UNSUPPORTED, "the shared-memory kernel is float64 only");
+    if (params->engine == LQMC_ENGINE_TILED && params->mode == LQMC_MODE_COMPAT)
+        return fail(nullptr, LQMC_ERR_UNSUPPORTED, "compat mode runs on the shared-memory kernel only");
     if (params->stab_every < 0 || params->delay < 0)
         return fail(nullptr, LQMC_ERR_INVALID, "negative stab_every or delay");
     if (params->precision == LQMC_PREC_MIXED && params->mode == LQMC_MODE_COMPAT)
         return fail(nullptr, LQMC_ERR_UNSUPPORTED, "compat mode replays float64 arithmetic only");
-    if (params->precision == LQMC_PREC_MIXED)
-        return fail(nullptr, LQMC_ERR_UNSUPPORTED, "mixed precision is not available in this build");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess) return fail(nullptr, LQMC_ERR_CUDA, std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e));
@@ -172,8 +185,14 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
     for (int c = 0; c < n_chains; ++c) {
         if (n_sites[c] < 1 || n_slices[c] < 1)
             return fail(h, LQMC_ERR_INVALID, "chain " + std::to_string(c) + ": n_sites and n_slices must be >= 1");
-        if (n_sites[c] > kMaxSitesFp64)
-            return fail(h, LQMC_ERR_UNSUPPORTED, "chain " + std::to_string(c) + ": n_sites > 128 needs the tiled engine");
+        if (h->p.mode == LQMC_MODE_COMPAT && n_sites[c] > kMaxSitesSmem)
+            return fail(h, LQMC_ERR_UNSUPPORTED, "chain " + std::to_string(c) +
+                        ": compat mode runs on the shared-memory kernel, n_sites <= 128");
+        if (h->p.engine == LQMC_ENGINE_SMEM && n_sites[c] > kMaxSitesSmem)
+            return fail(h, LQMC_ERR_UNSUPPORTED, "chain " + std::to_string(c) +
+                        ": the shared-memory kernel holds n_sites <= 128");
+        if (n_sites[c] > kMaxSitesTiled)
+            return fail(h, LQMC_ERR_UNSUPPORTED, "chain " + std::to_string(c) + ": n_sites > 2048");
         if (!exp_k[c] || !exp_k_inv[c] || !kinetic[c])
             return fail(h, LQMC_ERR_INVALID, "chain " + std::to_string(c) + ": null matrix");
     }
@@ -201,6 +220,7 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
     // layout of the float64 arena
     std::vector<size_t> off(n_chains);
     std::vector<size_t> smem(n_chains);
+    std::vector<int> kind(n_chains);
     size_t total = 0, total_i8 = 0;
     std::vector<size_t> off_i8(n_chains);
     for (int c = 0; c < n_chains; ++c) {
@@ -219,15 +239,32 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
         for (int k = 0; k < 4; ++k) d.c[k] = exp_consts[4 * c + k];
         d.u = u[c];
         d.drift_tol = 1e-6;
-        int flags = 0;
-        if (lqmc::sweep_fp64_smem_bytes(n, flags) > smem_cap) flags = lqmc::kScratchInGlobal;
-        if (lqmc::sweep_fp64_smem_bytes(n, flags) > smem_cap) flags |= lqmc::kGreenInGlobal;
-        d.flags = flags;
-        smem[c] = lqmc::sweep_fp64_smem_bytes(n, flags);
-        size_t work = (size_t)(2 * d.n_chunks + 4) * d.slot;
-        if (flags & lqmc::kGreenInGlobal) work += 2 * nn;
-        if (flags & lqmc::kScratchInGlobal) work += 2 * nn;
-        const size_t need = round_up(nn, kAlign) * 5 + round_up(2 * nn, kAlign) +
+        if (h->p.precision == LQMC_PREC_MIXED) kind[c] = kTiledFp32;
+        else if (h->p.engine == LQMC_ENGINE_TILED) kind[c] = kTiledFp64;
+        else kind[c] = (n <= kMaxSitesSmem) ? kSmemFp64 : kTiledFp64;
+        if (kind[c] == kSmemFp64 && h->p.engine == LQMC_ENGINE_SMEM && n > kMaxSitesSmem) {
+            release(h);
+            return fail(h, LQMC_ERR_UNSUPPORTED, "the shared-memory kernel holds n_sites <= 128");
+        }
+        size_t work = 0;
+        if (kind[c] == kSmemFp64) {
+            int flags = 0;
+            if (lqmc::sweep_fp64_smem_bytes(n, flags) > smem_cap) flags = lqmc::kScratchInGlobal;
+            if (lqmc::sweep_fp64_smem_bytes(n, flags) > smem_cap) flags |= lqmc::kGreenInGlobal;
+            d.flags = flags;
+            smem[c] = lqmc::sweep_fp64_smem_bytes(n, flags);
+            work = (size_t)(2 * d.n_chunks + 4) * d.slot;
+            if (flags & lqmc::kGreenInGlobal) work += 2 * nn;
+            if (flags & lqmc::kScratchInGlobal) work += 2 * nn;
+        } else {
+            const bool f32 = kind[c] == kTiledFp32;
+            d.flags = 0;
+            smem[c] = lqmc::sweep_tiled_smem_bytes(n, f32);
+            work = (lqmc::sweep_tiled_work_bytes(n, d.n_chunks, f32) + 7) / 8;
+            if (smem[c] > smem_cap) { release(h); return fail(h, LQMC_ERR_UNSUPPORTED, "lattice too large for shared memory"); }
+        }
+        const size_t fcopy = (kind[c] == kTiledFp32) ? 2 * round_up((nn + 1) / 2, kAlign) : 0;
+        const size_t need = round_up(nn, kAlign) * 5 + fcopy + round_up(2 * nn, kAlign) +
                             round_up(LQMC_OBS_LEN(n), kAlign) + round_up(LQMC_DIAG_LEN, kAlign) +
                             round_up(work, kAlign);
         off[c] = total;
@@ -260,6 +297,12 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
         double* eki = take(nn);
         double* ekit = take(nn);
         double* kin = take(nn);
+        float* ekf = nullptr;
+        float* ekif = nullptr;
+        if (kind[c] == kTiledFp32) {
+            ekf = reinterpret_cast<float*>(take((nn + 1) / 2));
+            ekif = reinterpret_cast<float*>(take((nn + 1) / 2));
+        }
         d.green = h->d_green + h->green_off[c];
         d.gsum = take(2 * nn);
         d.obs = take(LQMC_OBS_LEN(n));
@@ -282,14 +325,25 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
             for (int j = 0; j < n; ++j) tmp[(size_t)j * n + i] = exp_k_inv[c][(size_t)i * n + j];
         LQMC_CK(h, cudaMemcpy(ekit, tmp.data(), nn * sizeof(double), cudaMemcpyHostToDevice));
         LQMC_CK(h, cudaMemcpy(kin, kinetic[c], nn * sizeof(double), cudaMemcpyHostToDevice));
+        if (ekf) {
+            std::vector<float> tf(nn);
+            for (size_t e = 0; e < nn; ++e) tf[e] = (float)exp_k[c][e];
+            LQMC_CK(h, cudaMemcpy(ekf, tf.data(), nn * sizeof(float), cudaMemcpyHostToDevice));
+            for (size_t e = 0; e < nn; ++e) tf[e] = (float)exp_k_inv[c][e];
+            LQMC_CK(h, cudaMemcpy(ekif, tf.data(), nn * sizeof(float), cudaMemcpyHostToDevice));
+        }
+        d.expk_f = ekf;
+        d.expkinv_f = ekif;
     }
 
     // buckets of equal shared-memory footprint, largest first
-    std::map<size_t, std::vector<int>, std::greater<size_t>> groups;
-    for (int c = 0; c < n_chains; ++c) groups[smem[c]].push_back(c);
+    // buckets of one kernel and one shared-memory footprint; the largest lattices first
+    std::map<std::pair<int, size_t>, std::vector<int>> groups;
+    for (int c = 0; c < n_chains; ++c) groups[{-h->desc[c].n, (size_t)kind[c]}].push_back(c);
     for (auto& kv : groups) {
         Bucket b;
-        b.smem = kv.first;
+        b.kind = (int)kv.first.second;
+        b.smem = smem[kv.second[0]];
         b.chains = kv.second;
         e = cudaMalloc(&b.d_descs, sizeof(ChainDesc) * b.chains.size());
         if (e != cudaSuccess) { h->buckets.push_back(b); release(h); return fail(h, LQMC_ERR_NOMEM, "descriptor allocation failed"); }
@@ -444,15 +498,20 @@ int lqmc_sweep(lqmc_handle* h, int32_t n_sweeps, int32_t measure, void* stream_p
         }
         h->descs_dirty = false;
     }
+    auto launch = [&](Bucket& b, cudaStream_t st) {
+        if (b.kind == kSmemFp64)
+            return lqmc::launch_sweep_fp64(b.d_descs, (int)b.chains.size(), b.smem, n_sweeps, measure, st);
+        return lqmc::launch_sweep_tiled(b.d_descs, (int)b.chains.size(), b.smem, b.kind == kTiledFp32,
+                                        n_sweeps, measure, st);
+    };
     if (h->buckets.size() == 1) {
-        Bucket& b = h->buckets[0];
-        LQMC_CK(h, lqmc::launch_sweep_fp64(b.d_descs, (int)b.chains.size(), b.smem, n_sweeps, measure, stream));
+        LQMC_CK(h, launch(h->buckets[0], stream));
         ++h->launches;
     } else {
         LQMC_CK(h, cudaEventRecord(h->fork, stream));
         for (auto& b : h->buckets) {
             LQMC_CK(h, cudaStreamWaitEvent(b.stream, h->fork, 0));
-            LQMC_CK(h, lqmc::launch_sweep_fp64(b.d_descs, (int)b.chains.size(), b.smem, n_sweeps, measure, b.stream));
+            LQMC_CK(h, launch(b, b.stream));
             LQMC_CK(h, cudaEventRecord(b.done, b.stream));
             LQMC_CK(h, cudaStreamWaitEvent(stream, b.done, 0));
             ++h->launches;

@@ -39,6 +39,8 @@ struct ChainDesc {
     const double* uniforms;   // replay: [n_sweeps][n L]
     int8_t* decisions;        // [n_sweeps][L][n] (record)
     int32_t* status;          // LQMC_STATUS_* bits
+    const float* expk_f;      // float copies of expk / expkinv (mixed-precision engine)
+    const float* expkinv_f;
 };
 
 }  // namespace lqmc

@@ -493,26 +493,39 @@ sweep_fp64_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_meas
     double max_resid = 0.0;
     double logdet[2] = {0.0, 0.0}, sgn[2] = {1.0, 1.0};
     uint64_t sweep_id = (uint64_t)d.diag[7];
+    long long ph[5] = {0, 0, 0, 0, 0};   // clock cycles per phase (thread 0)
+    long long tc = clock64();
+#define LQMC_PHASE(k)                       \
+    do {                                    \
+        __syncthreads();                    \
+        const long long t_ = clock64();     \
+        ph[k] += t_ - tc;                   \
+        tc = t_;                            \
+    } while (0)
     for (int sw = 0; sw < n_sweeps; ++sw, ++sweep_id) {
         if (d.mode == LQMC_MODE_COMPAT) {
             compat_recompute(d, sm, 0, &singular);
             compat_recompute(d, sm, 1, &singular);
+            LQMC_PHASE(0);
             for (int l = d.L - 1; l >= 0; --l) {
                 update_slice(d, sm, l, sw, sweep_id, &accepted);
-                __syncthreads();
+                LQMC_PHASE(1);
                 if (l > 0) compat_wrap(d, sm, l - 1);
+                LQMC_PHASE(2);
             }
         } else {
             dqmc_right_stack(d, sm, 0, &logdet[0], &sgn[0], &singular);
             dqmc_right_stack(d, sm, 1, &logdet[1], &sgn[1], &singular);
+            LQMC_PHASE(0);
             int lp[2] = {0, 0};
             for (int c = d.n_chunks - 1; c >= 0; --c) {
                 const int lo = c * d.stab_every;
                 const int hi = min(lo + d.stab_every, d.L);
                 for (int l = hi - 1; l >= lo; --l) {
                     update_slice(d, sm, l, sw, sweep_id, &accepted);
-                    __syncthreads();
+                    LQMC_PHASE(1);
                     if (l > 0) dqmc_wrap(d, sm, l);
+                    LQMC_PHASE(2);
                 }
                 if (c > 0) {
                     for (int s = 0; s < 2; ++s) {
@@ -526,11 +539,14 @@ sweep_fp64_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_meas
                                                    &logdet[s], &sgn[s], &singular);
                         max_resid = fmax(max_resid, r);
                     }
+                    LQMC_PHASE(3);
                 }
             }
         }
         __syncthreads();
         if (do_measure) measure(d, sm);
+        LQMC_PHASE(4);
+#undef LQMC_PHASE
         // health check of G (NaN/Inf)
         int bad = 0;
         for (int e = threadIdx.x; e < 2 * nn; e += kNT) {
@@ -553,6 +569,7 @@ sweep_fp64_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_meas
         d.diag[5] = sgn[0];
         d.diag[6] = sgn[1];
         d.diag[7] += (double)n_sweeps;
+        for (int k = 0; k < 5; ++k) d.diag[8 + k] = (double)ph[k];
         if (singular) atomicOr(d.status, LQMC_STATUS_SINGULAR);
         if (max_resid > d.drift_tol) atomicOr(d.status, LQMC_STATUS_DRIFT);
     }

@@ -1,0 +1,674 @@
+// Persistent dqmc sweep kernel for large lattices and for mixed precision: one CTA per
+// Markov chain, every n x n matrix in global memory (L2-resident for tens of chains at
+// N = 256), dense products through the block-tiled GEMM of block_gemm.cuh.
+//
+// Template parameter T is the precision of G, of the wraps, of the rank-1 updates and of
+// the B-chain products (float: the mixed-precision engine; double: the plain FP64 engine).
+// The pre-pivoted Householder QR of the UDT chain product and the LU solve of the
+// stabilised inverse are float64 in both.  Same algorithm, sweep order and uniform stream
+// as the dqmc path of sweep_fp64.cu (lqmc/lqmc.py:301-347 with the defects fixed):
+//   ratio R = (1 + D_up (1 - G_up,ii)) (1 + D_dn (1 - G_dn,ii)), accept if u <= R
+//   G' = G - (D/R) G[:, i] (e_i - G[i, :])                 rank-1 update
+//   G <- e^{+dtau K} e^{-V_l} G e^{V_l} e^{-dtau K}         wrap from slice l to l-1
+//   refresh every stab_every slices from the UDT right stack and left product.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "block_fp64.cuh"
+#include "block_gemm.cuh"
+#include "chain_desc.h"
+#include "lqmc_gpu.h"
+#include "philox.cuh"
+
+namespace lqmc {
+namespace {
+
+using namespace blk;
+
+__host__ __device__ constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }
+
+// Per-chain global work layout of the tiled kernel (bytes from desc.work).
+template <typename T>
+struct TiledLayout {
+    size_t nn, g, z, s, slot, total;
+    __host__ __device__ TiledLayout(int n, int n_chunks) {
+        nn = (size_t)n * n;
+        g = 0;                                              // G_up, G_dn          (T)
+        z = g + align256(2 * nn * sizeof(T));               // Z0, Z1 GEMM temps   (T)
+        s = z + align256(2 * nn * sizeof(T));               // S0, S1 QR / LU      (double)
+        const size_t slots = s + align256(2 * nn * sizeof(double));
+        slot = align256(2 * nn * sizeof(T) + (size_t)(n + 1) * sizeof(double));
+        total = slots + (size_t)(2 * n_chunks + 4) * slot;
+        g_slots = slots;
+    }
+    size_t g_slots;
+};
+
+template <typename T>
+struct TSmem {
+    T* g[2];
+    T* z0;
+    T* z1;
+    double* s0;
+    double* s1;
+    unsigned char* slots;
+    size_t slot_bytes;
+    double* xv[2];
+    double* yv[2];
+    double* ev;
+    double* nrm;
+    double* tau;
+    double* dv;
+    int* order;
+    double* sv;
+    T* ev_t;      // exp_v of the current slice in precision T
+    T* iev_t;     // its inverse
+    T* xt[2];     // rank-1 update vectors in precision T
+    T* yt[2];
+    T* stage;
+};
+
+template <typename T> __device__ __forceinline__ T* slot_U(const TSmem<T>& sm, int idx, size_t nn) {
+    return reinterpret_cast<T*>(sm.slots + (size_t)idx * sm.slot_bytes);
+}
+template <typename T> __device__ __forceinline__ T* slot_T(const TSmem<T>& sm, int idx, size_t nn) {
+    return slot_U(sm, idx, nn) + nn;
+}
+template <typename T> __device__ __forceinline__ double* slot_d(const TSmem<T>& sm, int idx, size_t nn) {
+    return reinterpret_cast<double*>(slot_U(sm, idx, nn) + 2 * nn);
+}
+
+template <typename T> __device__ __forceinline__ const T* mat_expk(const ChainDesc& d);
+template <> __device__ __forceinline__ const double* mat_expk<double>(const ChainDesc& d) { return d.expk; }
+template <> __device__ __forceinline__ const float* mat_expk<float>(const ChainDesc& d) { return d.expk_f; }
+template <typename T> __device__ __forceinline__ const T* mat_expkinv(const ChainDesc& d);
+template <> __device__ __forceinline__ const double* mat_expkinv<double>(const ChainDesc& d) { return d.expkinv; }
+template <> __device__ __forceinline__ const float* mat_expkinv<float>(const ChainDesc& d) { return d.expkinv_f; }
+
+// exp_v of slice l, sigma (lqmc.py:149-154) in float64 and in T, and its inverse in T
+template <typename T>
+__device__ __forceinline__ void load_ev_t(const ChainDesc& d, TSmem<T>& sm, int l, int sigma) {
+    const int8_t* f = d.field + (size_t)l * d.n;
+    for (int j = threadIdx.x; j < d.n; j += kNT) {
+        const bool pos = sigma * f[j] > 0;
+        sm.ev[j] = pos ? d.c[2] : d.c[3];
+        sm.ev_t[j] = (T)(pos ? d.c[2] : d.c[3]);
+        sm.iev_t[j] = (T)(pos ? d.c[3] : d.c[2]);
+    }
+}
+
+// Householder QR in place of a column-major matrix (element (i, j) at s[j n + i], so that
+// every column is contiguous in global memory); same convention as blk::householder_qr.
+__device__ int householder_qr_cm(double* s, double* tau, int n, double* sv) {
+    const int lane = lane_id();
+    int nrefl = 0;
+    for (int j = 0; j < n - 1; ++j) {
+        double* cj = s + (size_t)j * n;
+        if (warp_id() == 0) {
+            double ss = 0.0;
+            for (int i = j + 1 + lane; i < n; i += 32) { const double v = cj[i]; ss = fma(v, v, ss); }
+            ss = warp_sum(ss);
+            if (lane == 0) {
+                const double alpha = cj[j];
+                const double xnorm = sqrt(ss);
+                if (xnorm == 0.0) {
+                    tau[j] = 0.0;
+                } else {
+                    const double beta = -copysign(hypot(alpha, xnorm), alpha);
+                    tau[j] = (beta - alpha) / beta;
+                    sv[kNW] = alpha - beta;
+                    sv[kNW + 1] = beta;
+                }
+            }
+        }
+        __syncthreads();
+        const double t = tau[j];
+        if (t == 0.0) continue;
+        ++nrefl;
+        const double den = sv[kNW];
+        for (int i = j + 1 + threadIdx.x; i < n; i += kNT) cj[i] = cj[i] / den;
+        __syncthreads();
+        for (int k = j + 1 + warp_id(); k < n; k += kNW) {
+            double* ck = s + (size_t)k * n;
+            double acc = 0.0;
+            for (int i = j + 1 + lane; i < n; i += 32) acc = fma(cj[i], ck[i], acc);
+            acc = warp_sum(acc);
+            const double wk = t * (ck[j] + acc);
+            for (int i = j + lane; i < n; i += 32) {
+                const double vi = (i == j) ? 1.0 : cj[i];
+                ck[i] = fma(-vi, wk, ck[i]);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) cj[j] = sv[kNW + 1];
+        __syncthreads();
+    }
+    return nrefl;
+}
+
+// Q = H_0 ... H_{n-2} in precision T, column-major (qc[k n + i] = Q[i][k]), from the
+// float64 column-major reflectors in s / tau.
+template <typename T>
+__device__ void form_q_cm_t(T* qc, const double* s, const double* tau, int n) {
+    const int lane = lane_id();
+    for (int k = warp_id(); k < n; k += kNW)
+        for (int i = lane; i < n; i += 32) qc[(size_t)k * n + i] = (i == k) ? T(1) : T(0);
+    __syncthreads();
+    for (int j = n - 2; j >= 0; --j) {
+        const T t = (T)tau[j];
+        if (t == T(0)) continue;
+        const double* vj = s + (size_t)j * n;
+        for (int k = j + warp_id(); k < n; k += kNW) {
+            T* qk = qc + (size_t)k * n;
+            T acc = T(0);
+            for (int i = j + 1 + lane; i < n; i += 32) acc = fma((T)vj[i], qk[i], acc);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            const T wk = t * (qk[j] + acc);
+            for (int i = j + lane; i < n; i += 32) {
+                const T vi = (i == j) ? T(1) : (T)vj[i];
+                qk[i] = fma(-vi, wk, qk[i]);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// UDT of Z diag(d_old) T_old (pre-pivoted QR, QR in float64).  z row-major; U is written
+// column-major (uc[k n + i] = U[i][k]), T row-major.  Returns det sign of U.
+template <typename T>
+__device__ double udt_absorb_t(const ChainDesc& d, TSmem<T>& sm, const T* z, const double* d_old,
+                               const T* t_old, T* u_new, double* d_new, T* t_new) {
+    const int n = d.n, lane = lane_id();
+    // column norms of Z diag(d_old): lanes over columns (contiguous rows of z)
+    for (int k = threadIdx.x; k < n; k += kNT) sm.nrm[k] = 0.0;
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += kNT) {
+        double acc = 0.0;
+        for (int i = 0; i < n; ++i) { const double v = (double)z[(size_t)i * n + k]; acc = fma(v, v, acc); }
+        const double dk = d_old ? fabs(d_old[k]) : 1.0;
+        sm.nrm[k] = sqrt(acc) * dk;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += kNT) {
+        const double v = isnan(sm.nrm[k]) ? -1.0 : sm.nrm[k];
+        int rank = 0;
+        for (int j = 0; j < n; ++j) {
+            const double w = isnan(sm.nrm[j]) ? -1.0 : sm.nrm[j];
+            rank += (w > v) || (w == v && j < k);
+        }
+        sm.order[rank] = k;
+    }
+    __syncthreads();
+    double* s = sm.s0;   // column-major
+    for (int i = warp_id(); i < n; i += kNW)
+        for (int r = lane; r < n; r += 32) {
+            const int src = sm.order[r];
+            s[(size_t)r * n + i] = (double)z[(size_t)i * n + src] * (d_old ? d_old[src] : 1.0);
+        }
+    __syncthreads();
+    const int nrefl = householder_qr_cm(s, sm.tau, n, sm.sv);
+    for (int i = threadIdx.x; i < n; i += kNT) {
+        const double di = s[(size_t)i * n + i];
+        sm.dv[i] = di;
+        d_new[i] = di;
+    }
+    __syncthreads();
+    form_q_cm_t<T>(u_new, s, sm.tau, n);
+    __syncthreads();
+    for (int k = warp_id(); k < n; k += kNW)
+        for (int i = lane; i <= k; i += 32) s[(size_t)k * n + i] = s[(size_t)k * n + i] / sm.dv[i];
+    __syncthreads();
+    for (int i = warp_id(); i < n; i += kNW) {
+        for (int c = lane; c < n; c += 32) {
+            T acc = T(0);
+            for (int k = i; k < n; ++k) {
+                const int src = sm.order[k];
+                const T tv = t_old ? t_old[(size_t)src * n + c] : (src == c ? T(1) : T(0));
+                acc = fma((T)s[(size_t)k * n + i], tv, acc);
+            }
+            t_new[(size_t)i * n + c] = acc;
+        }
+    }
+    __syncthreads();
+    return (nrefl & 1) ? -1.0 : 1.0;
+}
+
+// G = (1 + U_R D_R T_R T_L^T D_L U_L^T)^-1; ul == nullptr: identity left product.
+// U_R, U_L column-major (uc[k n + i] = U[i][k]), T_R, T_L row-major.
+template <typename T>
+__device__ double green_udt_t(const ChainDesc& d, TSmem<T>& sm, const T* ur, const double* dr,
+                              const T* tr, double sign_r, const T* ul, const double* dl,
+                              const T* tl, double sign_l, T* g, bool residual, double* logdet,
+                              double* sgn, int* singular) {
+    const int n = d.n, lane = lane_id();
+    double* dbr = sm.xv[0];
+    double* dsr = sm.xv[1];
+    double* dbl = sm.yv[0];
+    double* dsl = sm.yv[1];
+    for (int i = threadIdx.x; i < n; i += kNT) {
+        const double a = dr[i], b = fmax(fabs(a), 1.0);
+        dbr[i] = b;
+        dsr[i] = a / b;
+        if (ul) {
+            const double c = dl[i], e = fmax(fabs(c), 1.0);
+            dbl[i] = e;
+            dsl[i] = c / e;
+        } else {
+            dbl[i] = 1.0;
+            dsl[i] = 1.0;
+        }
+    }
+    if (ul) {
+        // X = U_R^T U_L: A(i,p) = U_R[p][i] = ur[i n + p]; B(p,j) = U_L[p][j] = ul[j n + p]
+        tile_gemm<T, false, true>(sm.z0, n, ur, n, ul, n, n, n, n, sm.stage);
+        tile_gemm<T, false, true>(sm.z1, n, tr, n, tl, n, n, n, n, sm.stage);   // Y = T_R T_L^T
+    }
+    __syncthreads();
+    for (int i = warp_id(); i < n; i += kNW)
+        for (int j = lane; j < n; j += 32) {
+            const size_t e = (size_t)i * n + j;
+            const double x = ul ? (double)sm.z0[e] : (double)ur[e];   // U_R^T[i][j] = ur[i n + j]
+            const double y = ul ? (double)sm.z1[e] : (double)tr[e];
+            sm.s0[e] = x / dbr[i] / dbl[j] + dsr[i] * y * dsl[j];
+            sm.s1[e] = (double)ur[e] / dbr[i];
+        }
+    __syncthreads();
+    double la, sw;
+    int sing;
+    lu_solve(sm.s0, sm.s1, n, sm.sv, &la, &sw, &sing);
+    if (sing) *singular = 1;
+    double res = 0.0, m = 0.0;
+    if (ul) {
+        for (int i = warp_id(); i < n; i += kNW)
+            for (int j = lane; j < n; j += 32) sm.s1[(size_t)i * n + j] /= dbl[i];
+        __syncthreads();
+        // G = U_L Z: A(i,p) = U_L[i][p] = ul[p n + i]
+        tile_gemm<T, true, false>(sm.z0, n, ul, n, sm.s1, n, n, n, n, sm.stage);
+        for (int i = warp_id(); i < n; i += kNW)
+            for (int j = lane; j < n; j += 32) {
+                const size_t e = (size_t)i * n + j;
+                if (residual) m = fmax(m, fabs((double)sm.z0[e] - (double)g[e]));
+                g[e] = sm.z0[e];
+            }
+    } else {
+        for (int i = warp_id(); i < n; i += kNW)
+            for (int j = lane; j < n; j += 32) {
+                const size_t e = (size_t)i * n + j;
+                if (residual) m = fmax(m, fabs(sm.s1[e] - (double)g[e]));
+                g[e] = (T)sm.s1[e];
+            }
+    }
+    if (residual) res = block_max(m, sm.sv);
+    double part = 0.0;
+    for (int i = threadIdx.x; i < n; i += kNT) part += log(dbr[i]) + log(dbl[i]);
+    const double tot = block_sum(part, sm.sv);
+    __syncthreads();
+    *logdet = -(tot + la);
+    *sgn = sign_r * sw * sign_l;
+    return res;
+}
+
+template <typename T>
+__device__ void right_stack_t(const ChainDesc& d, TSmem<T>& sm, int s, double* logdet, double* sgn,
+                              int* singular) {
+    const int n = d.n, sigma = s ? -1 : 1;
+    const size_t nn = (size_t)n * n;
+    const T* ek = mat_expk<T>(d);
+    for (int c = 0; c < d.n_chunks; ++c) {
+        const int lo = c * d.stab_every, hi = min(lo + d.stab_every, d.L);
+        const int prev = s * d.n_chunks + c - 1, cur = s * d.n_chunks + c;
+        T* za = sm.z0;
+        T* zb = sm.z1;
+        for (int l = lo; l < hi; ++l) {
+            load_ev_t<T>(d, sm, l, sigma);
+            __syncthreads();
+            GemmOpt<T> o;
+            o.rs = sm.ev_t;
+            if (l == lo && c == 0) {
+                // e^V e^{-dtau K}: the first factor itself
+                for (int i = warp_id(); i < n; i += kNW)
+                    for (int j = lane_id(); j < n; j += 32)
+                        zb[(size_t)i * n + j] = sm.ev_t[i] * ek[(size_t)i * n + j];
+                __syncthreads();
+            } else if (l == lo) {
+                // B(p, j) = U[p][j] = uc[j n + p] (column-major slot)
+                tile_gemm<T, false, true>(zb, n, ek, n, slot_U(sm, prev, nn), n, n, n, n, sm.stage, o);
+            } else {
+                tile_gemm<T, false, false>(zb, n, ek, n, za, n, n, n, n, sm.stage, o);   // e^V e^{-dtau K} Z
+            }
+            T* t = za; za = zb; zb = t;
+        }
+        const double sg = udt_absorb_t<T>(d, sm, za, c ? slot_d(sm, prev, nn) : nullptr,
+                                          c ? slot_T(sm, prev, nn) : nullptr, slot_U(sm, cur, nn),
+                                          slot_d(sm, cur, nn), slot_T(sm, cur, nn));
+        if (threadIdx.x == 0) slot_d(sm, cur, nn)[n] = sg;
+        __syncthreads();
+    }
+    const int top = s * d.n_chunks + d.n_chunks - 1;
+    green_udt_t<T>(d, sm, slot_U(sm, top, nn), slot_d(sm, top, nn), slot_T(sm, top, nn),
+                   slot_d(sm, top, nn)[n], nullptr, nullptr, nullptr, 1.0, sm.g[s], false, logdet,
+                   sgn, singular);
+}
+
+template <typename T>
+__device__ void left_step_t(const ChainDesc& d, TSmem<T>& sm, int s, int p_in, bool first, int lo,
+                            int hi) {
+    const int n = d.n, sigma = s ? -1 : 1;
+    const size_t nn = (size_t)n * n;
+    const int in = 2 * d.n_chunks + 2 * s + p_in, out = 2 * d.n_chunks + 2 * s + (1 - p_in);
+    const T* ek = mat_expk<T>(d);
+    T* za = sm.z0;
+    T* zb = sm.z1;
+    const int lane = lane_id();
+    for (int l = hi - 1; l >= lo; --l) {
+        load_ev_t<T>(d, sm, l, sigma);
+        __syncthreads();
+        if (l == hi - 1) {
+            // za = e^V U (U column-major in the slot; identity on the first chunk)
+            const T* u = slot_U(sm, in, nn);
+            for (int k = warp_id(); k < n; k += kNW)
+                for (int i = lane; i < n; i += 32)
+                    za[(size_t)i * n + k] = first ? (i == k ? sm.ev_t[i] : T(0))
+                                                  : sm.ev_t[i] * u[(size_t)k * n + i];
+        } else {
+            for (int i = warp_id(); i < n; i += kNW)
+                for (int j = lane; j < n; j += 32)
+                    za[(size_t)i * n + j] = sm.ev_t[i] * za[(size_t)i * n + j];
+        }
+        tile_gemm<T, true, false>(zb, n, ek, n, za, n, n, n, n, sm.stage);   // e^{-dtau K}^T (e^V Z)
+        T* t = za; za = zb; zb = t;
+    }
+    const double sg = udt_absorb_t<T>(d, sm, za, first ? nullptr : slot_d(sm, in, nn),
+                                      first ? nullptr : slot_T(sm, in, nn), slot_U(sm, out, nn),
+                                      slot_d(sm, out, nn), slot_T(sm, out, nn));
+    if (threadIdx.x == 0) slot_d(sm, out, nn)[n] = sg;
+    __syncthreads();
+}
+
+template <typename T>
+__device__ void wrap_t(const ChainDesc& d, TSmem<T>& sm, int l) {
+    const int n = d.n;
+    const size_t nn = (size_t)n * n;
+    for (int s = 0; s < 2; ++s) {
+        load_ev_t<T>(d, sm, l, s ? -1 : 1);
+        __syncthreads();
+        T* g = sm.g[s];
+        for (int i = warp_id(); i < n; i += kNW)
+            for (int j = lane_id(); j < n; j += 32) g[(size_t)i * n + j] *= sm.iev_t[i];
+        GemmOpt<T> o;
+        o.cs = sm.ev_t;
+        tile_gemm<T, false, false>(sm.z0, n, mat_expkinv<T>(d), n, g, n, n, n, n, sm.stage, o);
+        tile_gemm<T, false, false>(g, n, sm.z0, n, mat_expk<T>(d), n, n, n, n, sm.stage);
+    }
+}
+
+template <typename T>
+__device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int sw, uint64_t sweep_id,
+                               int* accepted) {
+    const int n = d.n, L = d.L, step = L - 1 - l;
+    const size_t nn = (size_t)n * n;
+    T* g0 = sm.g[0];
+    T* g1 = sm.g[1];
+    int8_t* f = d.field + (size_t)l * n;
+    for (int i = 0; i < n; ++i) {
+        const int pos = step * n + i;
+        const int8_t s_il = f[i];
+        double u;
+        if (d.rng == LQMC_RNG_REPLAY) u = d.uniforms[(size_t)sw * n * L + pos];
+        else u = philox_uniform(d.seed, (uint64_t)d.chain_id, sweep_id, (uint64_t)pos);
+        const double gi0 = (double)g0[(size_t)i * n + i], gi1 = (double)g1[(size_t)i * n + i];
+        const double ep = s_il > 0 ? d.c[0] : d.c[1];
+        const double em = s_il > 0 ? d.c[1] : d.c[0];
+        const double dl_up = ep - 1.0, dl_dn = em - 1.0;
+        const double r_up = 1.0 + dl_up * (1.0 - gi0), r_dn = 1.0 + dl_dn * (1.0 - gi1);
+        const double ratio = r_up * r_dn;
+        const bool acc = (u <= ratio);
+        if (d.record && threadIdx.x == 0) d.decisions[((size_t)sw * L + step) * n + i] = acc ? 1 : 0;
+        if (!acc) continue;
+        const double a0 = dl_up / r_up, a1 = dl_dn / r_dn;
+        const T ta0 = (T)a0, ta1 = (T)a1;
+        for (int j = threadIdx.x; j < n; j += kNT) {
+            sm.xt[0][j] = -g0[(size_t)j * n + i];
+            sm.xt[1][j] = -g1[(size_t)j * n + i];
+            sm.yt[0][j] = ((j == i ? T(1) : T(0)) - g0[(size_t)i * n + j]) * ta0;
+            sm.yt[1][j] = ((j == i ? T(1) : T(0)) - g1[(size_t)i * n + j]) * ta1;
+        }
+        __syncthreads();
+        for (int r = warp_id(); r < n; r += kNW) {
+            const T x0 = sm.xt[0][r], x1 = sm.xt[1][r];
+            T* r0 = g0 + (size_t)r * n;
+            T* r1 = g1 + (size_t)r * n;
+            for (int c = lane_id(); c < n; c += 32) {
+                r0[c] = fma(x0, sm.yt[0][c], r0[c]);
+                r1[c] = fma(x1, sm.yt[1][c], r1[c]);
+            }
+        }
+        if (threadIdx.x == 0) {
+            f[i] = (int8_t)(-s_il);
+            ++*accepted;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__device__ void measure_t(const ChainDesc& d, TSmem<T>& sm) {
+    const int n = d.n;
+    const size_t nn = (size_t)n * n;
+    const T* g0 = sm.g[0];
+    const T* g1 = sm.g[1];
+    double* obs = d.obs;
+    for (int i = warp_id(); i < n; i += kNW)
+        for (int j = lane_id(); j < n; j += 32) {
+            const size_t e = (size_t)i * n + j;
+            d.gsum[e] += (double)g0[e];
+            d.gsum[nn + e] += (double)g1[e];
+        }
+    double* nu = sm.xv[0];
+    double* nd = sm.xv[1];
+    for (int i = threadIdx.x; i < n; i += kNT) {
+        const double a = 1.0 - (double)g0[(size_t)i * n + i], b = 1.0 - (double)g1[(size_t)i * n + i];
+        nu[i] = a;
+        nd[i] = b;
+        obs[LQMC_OBS_HEADER + i] += a + b;
+        obs[LQMC_OBS_HEADER + n + i] += a * b;
+    }
+    __syncthreads();
+    double ek = 0.0, ep = 0.0, dc = 0.0, dn = 0.0;
+    for (int j = warp_id(); j < n; j += kNW)
+        for (int k = lane_id(); k < n; k += 32) {
+            const double kv = d.kinetic[(size_t)j * n + k];
+            if (kv != 0.0) {
+                const double del = (j == k) ? 1.0 : 0.0;
+                ek += kv * ((del - (double)g0[(size_t)k * n + j]) + (del - (double)g1[(size_t)k * n + j]));
+            }
+        }
+    for (int i = threadIdx.x; i < n; i += kNT) {
+        ep += (nu[i] - 0.5) * (nd[i] - 0.5);
+        dc += nu[i] * nd[i];
+        dn += nu[i] + nd[i];
+    }
+    ek = block_sum(ek, sm.sv);
+    ep = block_sum(ep, sm.sv);
+    dc = block_sum(dc, sm.sv);
+    dn = block_sum(dn, sm.sv);
+    if (threadIdx.x == 0) {
+        obs[0] += 1.0;
+        obs[1] += ek;
+        obs[2] += d.u * ep;
+        obs[3] += dc / n;
+        obs[4] += dn / n;
+    }
+    double* onn = obs + LQMC_OBS_HEADER + 2 * n;
+    double* osz = onn + nn;
+    for (int i = warp_id(); i < n; i += kNW)
+      for (int j = lane_id(); j < n; j += 32) {
+        const size_t e = (size_t)i * n + j;
+        const double del = (i == j) ? 1.0 : 0.0;
+        const double same = nu[i] * nu[j] + nd[i] * nd[j] +
+                            (del - (double)g0[(size_t)j * n + i]) * (double)g0[e] +
+                            (del - (double)g1[(size_t)j * n + i]) * (double)g1[e];
+        const double cross = nu[i] * nd[j] + nd[i] * nu[j];
+        onn[e] += same + cross;
+        osz[e] += 0.25 * (same - cross);
+    }
+    __syncthreads();
+}
+
+}  // namespace
+
+template <typename T>
+__global__ void __launch_bounds__(kNT, 1)
+sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_measure) {
+    extern __shared__ __align__(16) double smem[];
+    __shared__ ChainDesc d;
+    __shared__ int accepted;
+    __shared__ int singular;
+    if (threadIdx.x == 0) {
+        d = descs[blockIdx.x];
+        accepted = 0;
+        singular = 0;
+    }
+    __syncthreads();
+    const int n = d.n;
+    const size_t nn = (size_t)n * n;
+    TiledLayout<T> lay(n, d.n_chunks);
+    unsigned char* w = reinterpret_cast<unsigned char*>(d.work);
+    TSmem<T> sm;
+    sm.g[0] = reinterpret_cast<T*>(w + lay.g);
+    sm.g[1] = sm.g[0] + nn;
+    sm.z0 = reinterpret_cast<T*>(w + lay.z);
+    sm.z1 = sm.z0 + nn;
+    sm.s0 = reinterpret_cast<double*>(w + lay.s);
+    sm.s1 = sm.s0 + nn;
+    sm.slots = w + lay.g_slots;
+    sm.slot_bytes = lay.slot;
+    double* p = smem;
+    sm.sv = p; p += kNW + 8;
+    sm.xv[0] = p; p += n;
+    sm.xv[1] = p; p += n;
+    sm.yv[0] = p; p += n;
+    sm.yv[1] = p; p += n;
+    sm.ev = p; p += n;
+    sm.nrm = p; p += n;
+    sm.tau = p; p += n;
+    sm.dv = p; p += n;
+    sm.order = reinterpret_cast<int*>(p); p += n;
+    p = smem + (((p - smem) + 3) & ~(ptrdiff_t)3);
+    T* tp = reinterpret_cast<T*>(p);
+    sm.ev_t = tp; tp += n;
+    sm.iev_t = tp; tp += n;
+    sm.xt[0] = tp; tp += n;
+    sm.xt[1] = tp; tp += n;
+    sm.yt[0] = tp; tp += n;
+    sm.yt[1] = tp; tp += n;
+    p = reinterpret_cast<double*>(tp);
+    p = smem + (((p - smem) + 3) & ~(ptrdiff_t)3);
+    sm.stage = reinterpret_cast<T*>(p);
+
+    double max_resid = 0.0;
+    double logdet[2] = {0.0, 0.0}, sgn[2] = {1.0, 1.0};
+    uint64_t sweep_id = (uint64_t)d.diag[7];
+    long long ph[5] = {0, 0, 0, 0, 0};   // clock cycles per phase (thread 0)
+    long long tc = clock64();
+#define LQMC_PHASE(k)                       \
+    do {                                    \
+        __syncthreads();                    \
+        const long long t_ = clock64();     \
+        ph[k] += t_ - tc;                   \
+        tc = t_;                            \
+    } while (0)
+    for (int sw = 0; sw < n_sweeps; ++sw, ++sweep_id) {
+        right_stack_t<T>(d, sm, 0, &logdet[0], &sgn[0], &singular);
+        right_stack_t<T>(d, sm, 1, &logdet[1], &sgn[1], &singular);
+        LQMC_PHASE(0);
+        int lp[2] = {0, 0};
+        for (int c = d.n_chunks - 1; c >= 0; --c) {
+            const int lo = c * d.stab_every, hi = min(lo + d.stab_every, d.L);
+            for (int l = hi - 1; l >= lo; --l) {
+                update_slice_t<T>(d, sm, l, sw, sweep_id, &accepted);
+                LQMC_PHASE(1);
+                if (l > 0) wrap_t<T>(d, sm, l);
+                LQMC_PHASE(2);
+            }
+            if (c > 0) {
+                for (int s = 0; s < 2; ++s) {
+                    left_step_t<T>(d, sm, s, lp[s], c == d.n_chunks - 1, lo, hi);
+                    lp[s] ^= 1;
+                    const int rs = s * d.n_chunks + c - 1, ls = 2 * d.n_chunks + 2 * s + lp[s];
+                    const double r = green_udt_t<T>(
+                        d, sm, slot_U(sm, rs, nn), slot_d(sm, rs, nn), slot_T(sm, rs, nn),
+                        slot_d(sm, rs, nn)[n], slot_U(sm, ls, nn), slot_d(sm, ls, nn),
+                        slot_T(sm, ls, nn), slot_d(sm, ls, nn)[n], sm.g[s], true, &logdet[s],
+                        &sgn[s], &singular);
+                    max_resid = fmax(max_resid, r);
+                }
+                LQMC_PHASE(3);
+            }
+        }
+        __syncthreads();
+        if (do_measure) measure_t<T>(d, sm);
+        LQMC_PHASE(4);
+#undef LQMC_PHASE
+        int bad = 0;
+        for (size_t e = threadIdx.x; e < 2 * nn; e += kNT) {
+            const double v = (e < nn) ? (double)sm.g[0][e] : (double)sm.g[1][e - nn];
+            if (!isfinite(v)) bad = 1;
+        }
+        bad = __syncthreads_or(bad);
+        if (bad && threadIdx.x == 0) atomicOr(d.status, LQMC_STATUS_NONFINITE);
+    }
+    for (size_t e = threadIdx.x; e < nn; e += kNT) {
+        d.green[e] = (double)sm.g[0][e];
+        d.green[nn + e] = (double)sm.g[1][e];
+    }
+    if (threadIdx.x == 0) {
+        d.diag[0] += (double)accepted;
+        d.diag[1] += (double)n_sweeps * n * d.L;
+        d.diag[2] = max_resid;
+        d.diag[3] = logdet[0];
+        d.diag[4] = logdet[1];
+        d.diag[5] = sgn[0];
+        d.diag[6] = sgn[1];
+        d.diag[7] += (double)n_sweeps;
+        for (int k = 0; k < 5; ++k) d.diag[8 + k] = (double)ph[k];
+        if (singular) atomicOr(d.status, LQMC_STATUS_SINGULAR);
+        if (max_resid > d.drift_tol) atomicOr(d.status, LQMC_STATUS_DRIFT);
+    }
+}
+
+// bytes of dynamic shared memory / per-chain global work of the tiled kernel
+size_t sweep_tiled_smem_bytes(int n, bool fp32) {
+    size_t v = (size_t)(kNW + 8 + 9 * n);
+    v = (v + 3) & ~(size_t)3;                                   // doubles
+    const size_t tvec = 6 * (size_t)n * (fp32 ? 4 : 8);         // T vectors, bytes
+    v += ((tvec + 7) / 8 + 3) & ~(size_t)3;
+    return v * sizeof(double) + (fp32 ? tile_gemm_smem<float>() : tile_gemm_smem<double>());
+}
+
+size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32) {
+    return fp32 ? TiledLayout<float>(n, n_chunks).total : TiledLayout<double>(n, n_chunks).total;
+}
+
+cudaError_t launch_sweep_tiled(const ChainDesc* d_descs, int n_chains, size_t smem, bool fp32,
+                               int n_sweeps, int measure, cudaStream_t stream) {
+    if (fp32) {
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(sweep_tiled_kernel<float>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        sweep_tiled_kernel<float><<<n_chains, kNT, smem, stream>>>(d_descs, n_sweeps, measure);
+    } else {
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(sweep_tiled_kernel<double>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+        }
+        sweep_tiled_kernel<double><<<n_chains, kNT, smem, stream>>>(d_descs, n_sweeps, measure);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace lqmc

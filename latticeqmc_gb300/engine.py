@@ -74,19 +74,23 @@ class Engine:
 
     mode       'compat' (reference arithmetic, lqmc/lqmc.py:301-347) or 'dqmc' (textbook,
                stabilised)
-    precision  'fp64'
+    precision  'fp64', or 'mixed' (float32 G, wraps, updates and B-chain products; float64
+               Householder QR and LU of the stabilisation)
     rng        'replay' (uniforms uploaded per sweep) or 'philox' (on device)
+    engine     'auto', 'smem' (one CTA per chain, G in shared memory, fp64, N <= 128) or
+               'tiled' (matrices in global memory, tiled GEMMs; any N up to 2048)
     """
 
     def __init__(self, chains, mode="dqmc", precision="fp64", rng="philox", stab_every=None,
-                 delay=0, seed=0, record=False, device=0):
+                 delay=0, seed=0, record=False, device=0, engine="auto"):
         self.chains = list(chains)
         if stab_every is None:
             stab_every = auto_stab_every(self.chains)
         self.stab_every = int(stab_every)
         self.mode, self.precision, self.rng = mode, precision, rng
         self.record = bool(record)
-        self._h = _native.Handle(mode, precision, rng, stab_every, delay, seed, record, device)
+        self._h = _native.Handle(mode, precision, rng, stab_every, delay, seed, record, device,
+                                 engine)
         n = len(self.chains)
         n_sites = np.array([c.n for c in self.chains], dtype=np.int32)
         n_slices = np.array([c.L for c in self.chains], dtype=np.int32)
@@ -202,7 +206,9 @@ class Engine:
         d = np.empty(_native.DIAG_LEN)
         self._h.call("lqmc_get_diagnostics", int(chain), ptr(d))
         return {"accepted": d[0], "attempted": d[1], "max_residual": d[2],
-                "logdet": d[3:5].copy(), "sign": d[5:7].copy(), "sweeps": int(d[7])}
+                "logdet": d[3:5].copy(), "sign": d[5:7].copy(), "sweeps": int(d[7]),
+                "phase_cycles": {"recompute": d[8], "update": d[9], "wrap": d[10],
+                                 "stabilise": d[11], "measure": d[12]}}
 
     def status(self):
         s = np.empty(len(self.chains), dtype=np.int32)

@@ -42,9 +42,17 @@ def test_error_codes():
     assert lib.lqmc_get_green(eng._h.h, 1, _native.ptr(out)) == -1
     assert lib.lqmc_get_green(eng._h.h, -1, _native.ptr(out)) == -1
     eng.close()
-    # lattices above the shared-memory engine's limit in fp64
+    # lattices above the shared-memory kernel's limit: compat mode and engine="smem" refuse
+    big = ChainSpec(np.zeros((200, 200)), 4.0, 1.0, 10, np.ones((200, 10), np.int8))
     with pytest.raises(_native.LqmcError) as e:
-        Engine([ChainSpec(np.zeros((200, 200)), 4.0, 1.0, 10, np.ones((200, 10), np.int8))])
+        Engine([big], mode="compat", rng="replay")
+    assert e.value.code == -4
+    with pytest.raises(_native.LqmcError) as e:
+        Engine([big], mode="dqmc", engine="smem")
+    assert e.value.code == -4
+    # compat mode has no mixed-precision or tiled variant
+    with pytest.raises(_native.LqmcError) as e:
+        Engine([spec], mode="compat", precision="mixed", rng="replay")
     assert e.value.code == -4
     # bad enum in lqmc_create
     p = _native.Params(mode=7)
