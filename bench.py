@@ -1,17 +1,22 @@
 """Throughput benchmark of the DQMC sweep engine on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload batched_fp64]
+                    [--workload square16_beta8 | batched_fp64]
 
 A step is one sweep of every chain of the workload (one lqmc_sweep(1) call).  The metric
 is site-updates/s: sum over chains of N_c * L_c site-update attempts per sweep, divided by
-the time per sweep; sweeps/s is reported beside it.
+the time per sweep; sweeps/s is reported beside it.  Inputs are synthetic random HS fields
+(the reference's own runs start from random fields), t=1, mu=0, periodic square lattices.
 
-Workload batched_fp64 (the reference's batched-chains configuration): 512 independent
-chains, 128 each of 4x4, 6x6, 8x8 and 10x10 periodic square lattices, t=1, mu=0, U drawn
-per chain from {2, 4, 6}, beta=4, dtau=0.1 (L=40), textbook DQMC in float64, QR/UDV
-stabilisation every 5 slices, on-device Philox uniforms, HS fields from seeds 0..511.
-Inputs are synthetic (random HS fields), as the reference's own runs are.
+Workload square16_beta8 (default; the configuration the metric "batched mixed vs plain
+FP64 at max|dG| <= 1e-6" is quoted on): 64 chains of 16x16 (N=256), U=4, beta=8, dtau=0.1
+(L=80), dqmc, stabilisation every 8 slices, on-device Philox uniforms.  `value` is the
+float64 engine (the only one meeting the max|dG| bar); the mixed-precision engine's
+throughput, speed-up and measured max|dG| against float64 on identical inputs are in
+`mixed`.
+
+Workload batched_fp64: 512 chains, 128 each of 4x4, 6x6, 8x8, 10x10, U drawn per chain
+from {2, 4, 6}, beta=4, L=40, dqmc float64, stabilisation every 5 slices.
 
 value      device throughput with all state resident in HBM.
 e2e        the same sweeps through the public C ABI in replay mode (the drop-in path of
@@ -70,6 +75,23 @@ def workload_batched(rank=0, per_side=128):
                        "stab every 5, philox",
            "chains": len(specs), "sides": sides, "beta": beta, "L": L, "stab_every": 5,
            "precision": "fp64", "mode": "dqmc"}
+    return specs, cfg
+
+
+def workload_square16(rank=0, chains=64):
+    from latticeqmc_gb300 import ChainSpec, HubbardModel
+    side, beta, L, u = 16, 8.0, 80, 4.0
+    m = HubbardModel(u=u, t=1, mu=0)
+    m.build_square(side)
+    kin = m.ham_kinetic()
+    rng = np.random.default_rng(2000 + rank)
+    n = side * side
+    specs = [ChainSpec(kin, u, beta, L, (2 * rng.integers(0, 2, (n, L)) - 1).astype(np.int8))
+             for _ in range(chains)]
+    cfg = {"workload": f"square16_beta8: {chains} chains of 16x16 periodic (N=256), U=4, mu=0, "
+                       "beta=8, dtau=0.1 (L=80), dqmc, stab every 8, philox",
+           "chains": chains, "sides": [side], "beta": beta, "L": L, "stab_every": 8,
+           "precision": "fp64 (value) and mixed (reported in `mixed`)", "mode": "dqmc"}
     return specs, cfg
 
 
@@ -151,10 +173,14 @@ def _cpu_worker(args):
     field = (2 * rng.integers(0, 2, (n, L)) - 1).astype(np.int8)
     spec = ChainSpec(m.ham_kinetic(), u, beta, L, field)
     uni = rng.random(n * L)
-    # size the sample from a short probe so that it takes about `seconds`
-    probe = compat.time_sites(spec.exp_k, field.copy(), spec.lamb, uni, min(n * L, 2 * n))
-    sample = int(min(n * L, max(2 * n, seconds / max(probe, 1e-9))))
-    return side, compat.time_sites(spec.exp_k, field.copy(), spec.lamb, uni, sample), sample
+    # size the sample from a short probe so that it takes about `seconds`; the per-site
+    # cost is the slope between a sample and one twice as long, which removes the one-off
+    # from-scratch G at the start of the sweep
+    probe = compat.time_sites(spec.exp_k, field.copy(), spec.lamb, uni, min(n * L, 16))
+    s1 = int(min(n * L // 2, max(8, seconds / 3.0 / max(probe, 1e-9))))
+    t1 = compat.time_sites(spec.exp_k, field.copy(), spec.lamb, uni, s1) * s1
+    t2 = compat.time_sites(spec.exp_k, field.copy(), spec.lamb, uni, 2 * s1) * 2 * s1
+    return side, max(t2 - t1, 1e-9) / s1, 3 * s1
 
 
 def cpu_baseline(specs, cfg, seconds_per_size=2.5, cores=None):
@@ -222,83 +248,137 @@ def fp64_peak_tflops(torch):
     return best
 
 
-def run_ours(args, rank, world):
-    import torch
+def time_engine(torch, specs, precision, stab, steps, warmup, stream, seed, dev, world,
+                sample_clocks=False):
     from latticeqmc_gb300 import Engine
-    dev = int(os.environ.get("LOCAL_RANK", 0))
-    torch.cuda.set_device(dev)
-    specs, cfg = workload_batched(rank, args.per_size)
-    stab = cfg["stab_every"]
-    eng = Engine(specs, mode="dqmc", rng="philox", seed=12345 + 1000003 * rank, stab_every=stab,
-                 device=dev)
-    stream = torch.cuda.Stream()
-    sites = sum(c.n * c.L for c in specs)
-    # warm-up
-    for _ in range(args.warmup):
+    eng = Engine(specs, mode="dqmc", precision=precision, rng="philox", seed=seed,
+                 stab_every=stab, device=dev)
+    for _ in range(warmup):
         eng.sweep(1, stream=stream.cuda_stream)
     torch.cuda.synchronize()
     acc0 = [eng.diagnostics(c)["accepted"] for c in range(len(specs))]
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    clocks = ClockSampler(dev)
-    clocks.start()
+    clocks = ClockSampler(dev) if sample_clocks else None
+    if clocks:
+        clocks.start()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     start.record(stream)
     launches = 0
-    for _ in range(args.steps):
+    for _ in range(steps):
         eng.sweep(1, stream=stream.cuda_stream)
         launches += eng.launch_count()
     end.record(stream)
     end.synchronize()
     torch.cuda.synchronize()
-    clk = clocks.stop()
-    ms = start.elapsed_time(end) / args.steps
+    clk = clocks.stop() if clocks else None
+    ms = start.elapsed_time(end) / steps
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
         torch.distributed.barrier()
-    acc1 = [eng.diagnostics(c)["accepted"] for c in range(len(specs))]
-    accepted = [(b - a) / args.steps for a, b in zip(acc0, acc1)]
-    resid = max(eng.diagnostics(c)["max_residual"] for c in range(len(specs)))
-    status_bad = int(np.count_nonzero(eng.status()))
-    flops = algorithmic_flops(specs, accepted, stab)
+    diags = [eng.diagnostics(c) for c in range(len(specs))]
+    accepted = [(dg["accepted"] - a) / steps for a, dg in zip(acc0, diags)]
+    out = dict(ms=ms, launches=launches, clocks=clk, accepted=accepted,
+               resid=max(dg["max_residual"] for dg in diags),
+               status_bad=int(np.count_nonzero(eng.status() & 3)),
+               phases={k: float(np.mean([dg["phase_cycles"][k] for dg in diags]))
+                       for k in diags[0]["phase_cycles"]})
     eng.close()
+    return out
 
-    # end to end through the C ABI: replay uniforms in, every chain's G out, per step
-    eng2 = Engine(specs, mode="dqmc", rng="replay", stab_every=stab, device=dev)
-    total_uni = sites
+
+def green_difference(specs, stab, dev, sweeps=1):
+    """max|G_mixed - G_fp64| after `sweeps` sweeps from identical fields and uniforms."""
+    from latticeqmc_gb300 import Engine
+    rng = np.random.default_rng(77)
+    a = Engine(specs, mode="dqmc", precision="fp64", rng="replay", stab_every=stab, device=dev,
+               record=True)
+    b = Engine(specs, mode="dqmc", precision="mixed", rng="replay", stab_every=stab, device=dev,
+               record=True)
+    total = sum(c.n * c.L for c in specs)
+    for _ in range(sweeps):
+        u = rng.random(total)
+        a.set_uniforms_all(u)
+        b.set_uniforms_all(u)
+        a.sweep(1)
+        b.sweep(1)
+    ga, gb = a.green_all(), b.green_all()
+    same = [bool(np.array_equal(a.decisions(c), b.decisions(c))) for c in range(len(specs))]
+    dg = float(np.abs(ga - gb).max())
+    # chains whose decisions all agreed: the pure precision effect
+    off, dg_same = 0, 0.0
+    for c, sp in enumerate(specs):
+        k = 2 * sp.n * sp.n
+        if same[c]:
+            dg_same = max(dg_same, float(np.abs(ga[off:off + k] - gb[off:off + k]).max()))
+        off += k
+    a.close()
+    b.close()
+    return dict(max_dG=dg, max_dG_identical_decisions=dg_same if any(same) else None,
+                chains_with_identical_decisions=int(sum(same)), chains=len(specs))
+
+
+def time_e2e(torch, specs, stab, steps, warmup, stream, dev, world, rank):
+    from latticeqmc_gb300 import Engine
+    eng = Engine(specs, mode="dqmc", rng="replay", stab_every=stab, device=dev)
+    total_uni = sum(c.n * c.L for c in specs)
     total_g = sum(2 * c.n * c.n for c in specs)
-    steps_all = args.warmup + args.steps
+    steps_all = warmup + steps
     pin_u = torch.empty(steps_all * total_uni, dtype=torch.float64, pin_memory=True)
     pin_u.numpy()[:] = np.random.default_rng(rank).random(steps_all * total_uni)
     pin_g = torch.empty(total_g, dtype=torch.float64, pin_memory=True)
     u_np, g_np = pin_u.numpy(), pin_g.numpy()
-    for s in range(args.warmup):
-        eng2.set_uniforms_all(u_np[s * total_uni:(s + 1) * total_uni])
-        eng2.sweep(1, stream=stream.cuda_stream)
-        eng2.green_all(g_np)
+    for s in range(warmup):
+        eng.set_uniforms_all(u_np[s * total_uni:(s + 1) * total_uni])
+        eng.sweep(1, stream=stream.cuda_stream)
+        eng.green_all(g_np)
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
-    for s in range(args.warmup, steps_all):
-        eng2.set_uniforms_all(u_np[s * total_uni:(s + 1) * total_uni])
-        eng2.sweep(1, stream=stream.cuda_stream)
-        eng2.green_all(g_np)
+    for s in range(warmup, steps_all):
+        eng.set_uniforms_all(u_np[s * total_uni:(s + 1) * total_uni])
+        eng.sweep(1, stream=stream.cuda_stream)
+        eng.green_all(g_np)
     torch.cuda.synchronize()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / steps
     if world > 1:
         t = torch.tensor([e2e_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_ms = float(t.item())
-    eng2.close()
+    eng.close()
+    return e2e_ms, total_uni * 8, total_g * 8
 
+
+def run_ours(args, rank, world):
+    import torch
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    if args.workload == "batched_fp64":
+        specs, cfg = workload_batched(rank, args.per_size)
+    else:
+        specs, cfg = workload_square16(rank, args.chains)
+    stab = cfg["stab_every"]
+    stream = torch.cuda.Stream()
+    seed = 12345 + 1000003 * rank
+    main = time_engine(torch, specs, "fp64", stab, args.steps, args.warmup, stream, seed, dev,
+                       world, sample_clocks=True)
+    mixed = None
+    if args.workload == "square16_beta8":
+        mx = time_engine(torch, specs, "mixed", stab, args.steps, args.warmup, stream, seed, dev, world)
+        dg = green_difference(specs, stab, dev)
+        mixed = dict(ms_per_step=mx["ms"], status_flagged_chains=mx["status_bad"],
+                     max_stabilisation_residual=mx["resid"], **dg)
+    e2e_ms, h2d, d2h = time_e2e(torch, specs, stab, args.steps, args.warmup, stream, dev, world, rank)
     peak = fp64_peak_tflops(torch) if rank == 0 else None
-    return dict(ms=ms, sites=sites, chains=len(specs), flops=flops, launches=launches,
-                clocks=clk, e2e_ms=e2e_ms, h2d=total_uni * 8, d2h=total_g * 8, cfg=cfg,
-                resid=resid, status_bad=status_bad, peak=peak, specs=specs)
+    return dict(ms=main["ms"], sites=sum(c.n * c.L for c in specs), chains=len(specs),
+                flops=algorithmic_flops(specs, main["accepted"], stab), launches=main["launches"],
+                clocks=main["clocks"], e2e_ms=e2e_ms, h2d=h2d, d2h=d2h, cfg=cfg,
+                resid=main["resid"], status_bad=main["status_bad"], peak=peak, specs=specs,
+                phases=main["phases"], mixed=mixed)
 
 
 def main():
@@ -307,7 +387,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batched_fp64", choices=["batched_fp64"])
+    ap.add_argument("--workload", default="square16_beta8", choices=["square16_beta8", "batched_fp64"])
+    ap.add_argument("--chains", type=int, default=64, help="chains of the square16_beta8 workload")
     ap.add_argument("--cpu-seconds", type=float, default=2.5,
                     help="seconds of CPU sampling per lattice size and process")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -320,7 +401,10 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        specs, cfg = workload_batched(0, args.per_size)
+        if args.workload == "batched_fp64":
+            specs, cfg = workload_batched(0, args.per_size)
+        else:
+            specs, cfg = workload_square16(0, args.chains)
         vals = []
         last = None
         for s in range(args.warmup + args.steps):
@@ -359,8 +443,8 @@ def main():
             "sweeps_per_s": 1e3 / r["ms"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": dict(r["cfg"], parallelism=f"chains sharded over {world} GPU(s)",
-                           l2="working set (UDT stacks of 512 chains, ~1.6 GB) exceeds the "
-                              "129 MB L2; no flush"),
+                           l2="working set (per-chain G, GEMM temporaries and UDT stacks; "
+                              "0.6-1.6 GB) exceeds the 129 MB L2; no flush"),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"]},
             "gpu_launches": r["launches"],
@@ -369,12 +453,18 @@ def main():
                          "traffic": None,
                          "peak_source": "cuBLAS DGEMM 4096^3 measured in this run "
                                         "(MEASURED_PEAKS.json carries no float64 figure)",
-                         "kernel": "sweep_fp64_kernel (all launch buckets of one sweep)"},
+                         "kernel": "sweep kernel of the float64 engine (all launch buckets of one sweep)"},
             "cpu_baseline": cpu,
             "clocks": r["clocks"],
             "accuracy": {"max_stabilisation_residual": r["resid"],
                          "chains_with_status_flags": r["status_bad"]},
+            "phase_share": {k: v / max(sum(r["phases"].values()), 1.0) for k, v in r["phases"].items()},
         }
+        if r["mixed"]:
+            mx = r["mixed"]
+            line["mixed"] = dict(mx, value=sites_all / (mx["ms_per_step"] * 1e-3), unit=UNIT,
+                                 speedup_vs_fp64=r["ms"] / mx["ms_per_step"])
+            line["mixed"]["meets_max_dG_1e-6"] = bool(mx["max_dG"] <= 1e-6)
         print(json.dumps(line))
     if world > 1:
         import torch

@@ -1,8 +1,8 @@
 // Block-cooperative tiled GEMM for one CTA of blk::kNT (256) threads.
 //
 // C (m x n) = op(A) (m x k) * op(B) (k x n), row-major, generic pointers (global or shared
-// memory).  64 x 64 output tiles, 4 x 4 outputs per thread, k staged through shared memory
-// 16 at a time.  Every output is one fma chain in increasing k starting from zero, so the
+// memory).  Square output tiles (128 in float, 64 in double) with 8 x 8 / 4 x 4 outputs per
+// thread, k staged through shared memory 16 at a time.  Every output is one fma chain in increasing k starting from zero, so the
 // result is independent of the tiling.  Inputs of another type (float / double) are
 // converted when they are staged.  Epilogue options: scale rows (rs) and columns (cs) of
 // the product, and subtract the product from C instead of overwriting it.
@@ -14,13 +14,19 @@
 namespace lqmc {
 namespace blk {
 
-constexpr int kTile = 64;
 constexpr int kTileK = 16;
+
+// outputs per thread along each axis: 8 x 8 in float (128 x 128 tiles, 4 FMAs per shared
+// load), 4 x 4 in double (64 x 64 tiles; the float64 pipe is the limit there)
+template <typename T>
+constexpr int tile_r() { return sizeof(T) == 4 ? 8 : 4; }
+template <typename T>
+constexpr int tile_dim() { return 16 * tile_r<T>(); }
 
 // shared-memory bytes tile_gemm<T> needs for its staging buffers
 template <typename T>
 constexpr size_t tile_gemm_smem() {
-    return (size_t)2 * kTileK * (kTile + 1) * sizeof(T);
+    return (size_t)2 * kTileK * (tile_dim<T>() + 1) * sizeof(T);
 }
 
 template <typename T>
@@ -34,54 +40,56 @@ struct GemmOpt {
 template <typename T, bool TA, bool TB, typename TAIn, typename TBIn>
 __device__ void tile_gemm(T* __restrict__ c, int ldc, const TAIn* a, int lda, const TBIn* b,
                           int ldb, int m, int n, int k, T* stage, GemmOpt<T> opt = GemmOpt<T>()) {
-    T* as = stage;                              // [kTileK][kTile + 1], as[p][i] = A(i0 + i, p0 + p)
-    T* bs = stage + kTileK * (kTile + 1);       // [kTileK][kTile + 1], bs[p][j] = B(p0 + p, j0 + j)
+    constexpr int R = tile_r<T>();
+    constexpr int D = tile_dim<T>();
+    T* as = stage;                         // [kTileK][D + 1], as[p][i] = A(i0 + i, p0 + p)
+    T* bs = stage + kTileK * (D + 1);      // [kTileK][D + 1], bs[p][j] = B(p0 + p, j0 + j)
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-    const int tiles_m = (m + kTile - 1) / kTile, tiles_n = (n + kTile - 1) / kTile;
+    const int tiles_m = (m + D - 1) / D, tiles_n = (n + D - 1) / D;
     for (int tile = 0; tile < tiles_m * tiles_n; ++tile) {
-        const int i0 = (tile / tiles_n) * kTile, j0 = (tile % tiles_n) * kTile;
-        T acc[4][4];
+        const int i0 = (tile / tiles_n) * D, j0 = (tile % tiles_n) * D;
+        T acc[R][R];
 #pragma unroll
-        for (int r = 0; r < 4; ++r)
+        for (int r = 0; r < R; ++r)
 #pragma unroll
-            for (int s = 0; s < 4; ++s) acc[r][s] = T(0);
+            for (int s = 0; s < R; ++s) acc[r][s] = T(0);
         for (int p0 = 0; p0 < k; p0 += kTileK) {
             __syncthreads();
-            for (int e = threadIdx.x; e < kTileK * kTile; e += kNT) {
-                // A tile: element (i, p); consecutive threads walk the contiguous index
+            for (int e = threadIdx.x; e < kTileK * D; e += kNT) {
+                // consecutive threads walk the contiguous index of each operand
                 int i, p;
-                if (TA) { p = e / kTile; i = e % kTile; } else { i = e / kTileK; p = e % kTileK; }
+                if (TA) { p = e / D; i = e % D; } else { i = e / kTileK; p = e % kTileK; }
                 const int gi = i0 + i, gp = p0 + p;
                 T va = T(0);
                 if (gi < m && gp < k) va = (T)(TA ? a[(size_t)gp * lda + gi] : a[(size_t)gi * lda + gp]);
-                as[p * (kTile + 1) + i] = va;
+                as[p * (D + 1) + i] = va;
                 int q, j;
-                if (TB) { j = e / kTileK; q = e % kTileK; } else { q = e / kTile; j = e % kTile; }
+                if (TB) { j = e / kTileK; q = e % kTileK; } else { q = e / D; j = e % D; }
                 const int gq = p0 + q, gj = j0 + j;
                 T vb = T(0);
                 if (gq < k && gj < n) vb = (T)(TB ? b[(size_t)gj * ldb + gq] : b[(size_t)gq * ldb + gj]);
-                bs[q * (kTile + 1) + j] = vb;
+                bs[q * (D + 1) + j] = vb;
             }
             __syncthreads();
             const int pk = min(kTileK, k - p0);
             for (int p = 0; p < pk; ++p) {
-                T av[4], bv[4];
+                T av[R], bv[R];
 #pragma unroll
-                for (int r = 0; r < 4; ++r) av[r] = as[p * (kTile + 1) + ty + 16 * r];
+                for (int r = 0; r < R; ++r) av[r] = as[p * (D + 1) + ty + 16 * r];
 #pragma unroll
-                for (int s = 0; s < 4; ++s) bv[s] = bs[p * (kTile + 1) + tx + 16 * s];
+                for (int s = 0; s < R; ++s) bv[s] = bs[p * (D + 1) + tx + 16 * s];
 #pragma unroll
-                for (int r = 0; r < 4; ++r)
+                for (int r = 0; r < R; ++r)
 #pragma unroll
-                    for (int s = 0; s < 4; ++s) acc[r][s] = fma(av[r], bv[s], acc[r][s]);
+                    for (int s = 0; s < R; ++s) acc[r][s] = fma(av[r], bv[s], acc[r][s]);
             }
         }
 #pragma unroll
-        for (int r = 0; r < 4; ++r) {
+        for (int r = 0; r < R; ++r) {
             const int gi = i0 + ty + 16 * r;
             if (gi >= m) continue;
 #pragma unroll
-            for (int s = 0; s < 4; ++s) {
+            for (int s = 0; s < R; ++s) {
                 const int gj = j0 + tx + 16 * s;
                 if (gj >= n) continue;
                 T v = acc[r][s];

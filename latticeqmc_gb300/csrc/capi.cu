@@ -16,7 +16,8 @@ namespace lqmc {
 size_t sweep_fp64_smem_bytes(int n, int flags);
 cudaError_t launch_sweep_fp64(const ChainDesc* d_descs, int n_chains, size_t smem, int n_sweeps,
                               int measure, cudaStream_t stream);
-size_t sweep_tiled_smem_bytes(int n, bool fp32);
+size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay);
+int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap);
 size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32);
 cudaError_t launch_sweep_tiled(const ChainDesc* d_descs, int n_chains, size_t smem, bool fp32,
                                int n_sweeps, int measure, cudaStream_t stream);
@@ -27,7 +28,7 @@ using lqmc::ChainDesc;
 namespace {
 
 constexpr int kMaxSitesSmem = 128;    // one-CTA shared-memory kernel (both modes)
-constexpr int kMaxSitesTiled = 2048;  // tiled kernel (dqmc mode)
+constexpr int kMaxSitesTiled = 1024;  // tiled kernel (dqmc mode): 4 rows per thread
 
 // which sweep kernel runs a chain
 enum Kind : int { kSmemFp64 = 0, kTiledFp64 = 1, kTiledFp32 = 2 };
@@ -192,7 +193,7 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
             return fail(h, LQMC_ERR_UNSUPPORTED, "chain " + std::to_string(c) +
                         ": the shared-memory kernel holds n_sites <= 128");
         if (n_sites[c] > kMaxSitesTiled)
-            return fail(h, LQMC_ERR_UNSUPPORTED, "chain " + std::to_string(c) + ": n_sites > 2048");
+            return fail(h, LQMC_ERR_UNSUPPORTED, "chain " + std::to_string(c) + ": n_sites > 1024");
         if (!exp_k[c] || !exp_k_inv[c] || !kinetic[c])
             return fail(h, LQMC_ERR_INVALID, "chain " + std::to_string(c) + ": null matrix");
     }
@@ -259,7 +260,8 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
         } else {
             const bool f32 = kind[c] == kTiledFp32;
             d.flags = 0;
-            smem[c] = lqmc::sweep_tiled_smem_bytes(n, f32);
+            d.delay = lqmc::sweep_tiled_delay(n, f32, h->p.delay, smem_cap);
+            smem[c] = lqmc::sweep_tiled_smem_bytes(n, f32, d.delay);
             work = (lqmc::sweep_tiled_work_bytes(n, d.n_chunks, f32) + 7) / 8;
             if (smem[c] > smem_cap) { release(h); return fail(h, LQMC_ERR_UNSUPPORTED, "lattice too large for shared memory"); }
         }

@@ -41,6 +41,8 @@ struct ChainDesc {
     int32_t* status;          // LQMC_STATUS_* bits
     const float* expk_f;      // float copies of expk / expkinv (mixed-precision engine)
     const float* expkinv_f;
+    int32_t delay;            // tiled kernel: rank-k depth of the delayed updates (>= 1)
+    int32_t pad1;
 };
 
 }  // namespace lqmc

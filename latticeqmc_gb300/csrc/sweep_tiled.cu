@@ -66,6 +66,13 @@ struct TSmem {
     T* xt[2];     // rank-1 update vectors in precision T
     T* yt[2];
     T* stage;
+    T* dx[2];     // delayed updates: X_s (n x (kd + 1)), G_eff = G - X Y^T
+    T* dy[2];     // Y_s (n x (kd + 1))
+    double* gii;  // [2 parity][2 spins] diagonal of G_eff for the current site
+    long long* sub;   // [3] clock cycles: Householder QR, Q and T formation, LU solve
+    double* panel;    // blocked LU panel, n x (kPanel + 1); aliases dx/dy (not live then)
+    int* piv;         // [kPanel] panel pivots
+    double* stage64;  // float64 GEMM staging of the LU
 };
 
 template <typename T> __device__ __forceinline__ T* slot_U(const TSmem<T>& sm, int idx, size_t nn) {
@@ -146,6 +153,137 @@ __device__ int householder_qr_cm(double* s, double* tau, int n, double* sv) {
     return nrefl;
 }
 
+// Solve W Z = R in place (both n x n, row-major, global memory) by a blocked right-looking
+// LU with partial pivoting: each 32-column panel is factorised in shared memory (pivot =
+// first maximal |entry|, as LAPACK), its row interchanges applied across W and R, and the
+// trailing submatrix and R updated with tiled float64 GEMMs; then blocked back substitution.
+// `panel` is shared memory of n * (panel_width(n) + 1) doubles, `stage` the GEMM staging
+// buffer.  Returns log|det W|, sign(det W) and a zero-pivot flag like blk::lu_solve.
+constexpr int kPanel = 32;   // widest panel
+
+__host__ __device__ constexpr int panel_width(int n) { return n <= 256 ? 32 : (n <= 512 ? 16 : 8); }
+
+__device__ void lu_solve_blocked(double* w, double* rhs, int n, double* panel, int* piv,
+                                 double* stage, double* sv, double* logabs, double* sgn,
+                                 int* singular) {
+    const int lane = lane_id();
+    const int P = panel_width(n), LD = P + 1;
+    double la = 0.0, sg = 1.0;
+    int sing = 0;
+    for (int jb = 0; jb < n; jb += P) {
+        const int nb = min(P, n - jb), rows = n - jb;
+        // load the panel W[jb:n, jb:jb+nb] into shared memory: panel[r * LD + c]
+        for (int r = warp_id(); r < rows; r += kNW)
+            for (int c = lane; c < nb; c += 32) panel[r * LD + c] = w[(size_t)(jb + r) * n + jb + c];
+        __syncthreads();
+        // unblocked LU with partial pivoting inside the panel
+        for (int c = 0; c < nb; ++c) {
+            if (warp_id() == 0) {
+                double best = -1.0;
+                int bi = rows;
+                for (int r = c + lane; r < rows; r += 32) {
+                    const double v = fabs(panel[r * LD + c]);
+                    if (v > best) { best = v; bi = r; }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                    if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+                }
+                if (lane == 0) piv[c] = (bi < rows) ? bi : c;
+            }
+            __syncthreads();
+            const int p = piv[c];
+            if (p != c) {
+                for (int k = threadIdx.x; k < nb; k += kNT) {
+                    const double t = panel[c * LD + k];
+                    panel[c * LD + k] = panel[p * LD + k];
+                    panel[p * LD + k] = t;
+                }
+                sg = -sg;
+            }
+            __syncthreads();
+            const double pv = panel[c * LD + c];
+            if (pv == 0.0) sing = 1;
+            la += log(fabs(pv));
+            if (pv < 0.0) sg = -sg;
+            for (int r = c + 1 + threadIdx.x; r < rows; r += kNT) panel[r * LD + c] /= pv;
+            __syncthreads();
+            for (int r = c + 1 + warp_id(); r < rows; r += kNW) {
+                const double l = panel[r * LD + c];
+                for (int k = c + 1 + lane; k < nb; k += 32) panel[r * LD + k] = fma(-l, panel[c * LD + k], panel[r * LD + k]);
+            }
+            __syncthreads();
+        }
+        // store the factored panel and apply its interchanges to the other columns of W and to R
+        for (int r = warp_id(); r < rows; r += kNW)
+            for (int c = lane; c < nb; c += 32) w[(size_t)(jb + r) * n + jb + c] = panel[r * LD + c];
+        for (int c = 0; c < nb; ++c) {
+            const int p = piv[c];
+            if (p == c) continue;
+            double* ra = w + (size_t)(jb + c) * n;
+            double* rb = w + (size_t)(jb + p) * n;
+            for (int k = threadIdx.x; k < n; k += kNT) {
+                if (k >= jb && k < jb + nb) continue;
+                const double t = ra[k]; ra[k] = rb[k]; rb[k] = t;
+            }
+            double* qa = rhs + (size_t)(jb + c) * n;
+            double* qb = rhs + (size_t)(jb + p) * n;
+            for (int k = threadIdx.x; k < n; k += kNT) {
+                const double t = qa[k]; qa[k] = qb[k]; qb[k] = t;
+            }
+            __syncthreads();
+        }
+        __syncthreads();
+        // U12 = L11^-1 W[jb:jb+nb, jb+nb:n] and R1 = L11^-1 R[jb:jb+nb, :] (unit lower, by columns)
+        const int rest = n - jb - nb;
+        for (int k = threadIdx.x; k < rest + n; k += kNT) {
+            double* col = (k < rest) ? (w + (size_t)jb * n + jb + nb + k) : (rhs + (size_t)jb * n + (k - rest));
+            for (int r = 1; r < nb; ++r) {
+                double v = col[(size_t)r * n];
+                for (int q = 0; q < r; ++q) v = fma(-panel[r * LD + q], col[(size_t)q * n], v);
+                col[(size_t)r * n] = v;
+            }
+        }
+        __syncthreads();
+        if (rest > 0) {
+            GemmOpt<double> o;
+            o.subtract = true;
+            // W22 -= L21 U12 ; R2 -= L21 R1
+            tile_gemm<double, false, false>(w + (size_t)(jb + nb) * n + jb + nb, n,
+                                            w + (size_t)(jb + nb) * n + jb, n,
+                                            w + (size_t)jb * n + jb + nb, n, rest, rest, nb, stage, o);
+            tile_gemm<double, false, false>(rhs + (size_t)(jb + nb) * n, n, w + (size_t)(jb + nb) * n + jb, n,
+                                            rhs + (size_t)jb * n, n, rest, n, nb, stage, o);
+        }
+    }
+    // back substitution with U, 32-row blocks from the bottom
+    for (int jb = ((n - 1) / P) * P; jb >= 0; jb -= P) {
+        const int nb = min(P, n - jb);
+        // R1 = U11^-1 R1 (upper, by columns)
+        for (int k = threadIdx.x; k < n; k += kNT) {
+            double* col = rhs + (size_t)jb * n + k;
+            for (int r = nb - 1; r >= 0; --r) {
+                const double* ur = w + (size_t)(jb + r) * n + jb;
+                double v = col[(size_t)r * n];
+                for (int q = r + 1; q < nb; ++q) v = fma(-ur[q], col[(size_t)q * n], v);
+                col[(size_t)r * n] = v / ur[r];
+            }
+        }
+        __syncthreads();
+        if (jb > 0) {
+            GemmOpt<double> o;
+            o.subtract = true;
+            // R0 -= U01 R1
+            tile_gemm<double, false, false>(rhs, n, w + jb, n, rhs + (size_t)jb * n, n, jb, n, nb, stage, o);
+        }
+    }
+    *logabs = la;
+    *sgn = sg;
+    *singular = sing;
+}
+
 // Q = H_0 ... H_{n-2} in precision T, column-major (qc[k n + i] = Q[i][k]), from the
 // float64 column-major reflectors in s / tau.
 template <typename T>
@@ -207,7 +345,10 @@ __device__ double udt_absorb_t(const ChainDesc& d, TSmem<T>& sm, const T* z, con
             s[(size_t)r * n + i] = (double)z[(size_t)i * n + src] * (d_old ? d_old[src] : 1.0);
         }
     __syncthreads();
+    long long t0 = clock64();
     const int nrefl = householder_qr_cm(s, sm.tau, n, sm.sv);
+    long long t1 = clock64();
+    if (threadIdx.x == 0) sm.sub[0] += t1 - t0;
     for (int i = threadIdx.x; i < n; i += kNT) {
         const double di = s[(size_t)i * n + i];
         sm.dv[i] = di;
@@ -231,6 +372,7 @@ __device__ double udt_absorb_t(const ChainDesc& d, TSmem<T>& sm, const T* z, con
         }
     }
     __syncthreads();
+    if (threadIdx.x == 0) sm.sub[1] += clock64() - t1;
     return (nrefl & 1) ? -1.0 : 1.0;
 }
 
@@ -276,7 +418,9 @@ __device__ double green_udt_t(const ChainDesc& d, TSmem<T>& sm, const T* ur, con
     __syncthreads();
     double la, sw;
     int sing;
-    lu_solve(sm.s0, sm.s1, n, sm.sv, &la, &sw, &sing);
+    const long long t0 = clock64();
+    lu_solve_blocked(sm.s0, sm.s1, n, sm.panel, sm.piv, sm.stage64, sm.sv, &la, &sw, &sing);
+    if (threadIdx.x == 0) sm.sub[2] += clock64() - t0;
     if (sing) *singular = 1;
     double res = 0.0, m = 0.0;
     if (ul) {
@@ -403,21 +547,49 @@ __device__ void wrap_t(const ChainDesc& d, TSmem<T>& sm, int l) {
     }
 }
 
+// Site updates of slice l with delayed rank-k updates (k = d.delay): the accepted flips of
+// the slice accumulate as G_eff = G - X Y^T with x = G_eff[:, i], y = (D/R)(e_i - G_eff[i, :])
+// (the Sherman-Morrison update of lqmc.py:318-331 with the defects fixed); every k flips,
+// and at the end of the slice, G -= X Y^T as one tiled GEMM per spin.
 template <typename T>
 __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int sw, uint64_t sweep_id,
                                int* accepted) {
-    const int n = d.n, L = d.L, step = L - 1 - l;
-    const size_t nn = (size_t)n * n;
-    T* g0 = sm.g[0];
-    T* g1 = sm.g[1];
+    const int n = d.n, L = d.L, step = L - 1 - l, kd = d.delay, ld = kd + 1;
+    T* g[2] = {sm.g[0], sm.g[1]};
     int8_t* f = d.field + (size_t)l * n;
+    int m = 0;   // pending updates
+    constexpr int kPer = 4;   // rows per thread: n <= kPer * kNT
     for (int i = 0; i < n; ++i) {
+        // G[:, i] and G[i, :] of both spins, loaded before they are needed
+        T colv[2][kPer], rowv[2][kPer];
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const int j = threadIdx.x + q * kNT;
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                colv[s][q] = (j < n) ? g[s][(size_t)j * n + i] : T(0);
+                rowv[s][q] = (j < n) ? g[s][(size_t)i * n + j] : T(0);
+            }
+        }
+        double* gii = sm.gii + 2 * (i & 1);
+        if (warp_id() == 0) {
+            const int lane = lane_id();
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                T part = T(0);
+                for (int q = lane; q < m; q += 32) part = fma(sm.dx[s][(size_t)i * ld + q], sm.dy[s][(size_t)i * ld + q], part);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+                if (lane == 0) gii[s] = (double)(g[s][(size_t)i * n + i] - part);
+            }
+        }
+        __syncthreads();
         const int pos = step * n + i;
         const int8_t s_il = f[i];
         double u;
         if (d.rng == LQMC_RNG_REPLAY) u = d.uniforms[(size_t)sw * n * L + pos];
         else u = philox_uniform(d.seed, (uint64_t)d.chain_id, sweep_id, (uint64_t)pos);
-        const double gi0 = (double)g0[(size_t)i * n + i], gi1 = (double)g1[(size_t)i * n + i];
+        const double gi0 = gii[0], gi1 = gii[1];
         const double ep = s_il > 0 ? d.c[0] : d.c[1];
         const double em = s_il > 0 ? d.c[1] : d.c[0];
         const double dl_up = ep - 1.0, dl_dn = em - 1.0;
@@ -426,22 +598,22 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int sw, 
         const bool acc = (u <= ratio);
         if (d.record && threadIdx.x == 0) d.decisions[((size_t)sw * L + step) * n + i] = acc ? 1 : 0;
         if (!acc) continue;
-        const double a0 = dl_up / r_up, a1 = dl_dn / r_dn;
-        const T ta0 = (T)a0, ta1 = (T)a1;
-        for (int j = threadIdx.x; j < n; j += kNT) {
-            sm.xt[0][j] = -g0[(size_t)j * n + i];
-            sm.xt[1][j] = -g1[(size_t)j * n + i];
-            sm.yt[0][j] = ((j == i ? T(1) : T(0)) - g0[(size_t)i * n + j]) * ta0;
-            sm.yt[1][j] = ((j == i ? T(1) : T(0)) - g1[(size_t)i * n + j]) * ta1;
-        }
-        __syncthreads();
-        for (int r = warp_id(); r < n; r += kNW) {
-            const T x0 = sm.xt[0][r], x1 = sm.xt[1][r];
-            T* r0 = g0 + (size_t)r * n;
-            T* r1 = g1 + (size_t)r * n;
-            for (int c = lane_id(); c < n; c += 32) {
-                r0[c] = fma(x0, sm.yt[0][c], r0[c]);
-                r1[c] = fma(x1, sm.yt[1][c], r1[c]);
+        const T a[2] = {(T)(dl_up / r_up), (T)(dl_dn / r_dn)};
+#pragma unroll
+        for (int q = 0; q < kPer; ++q) {
+            const int j = threadIdx.x + q * kNT;
+            if (j >= n) break;
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                const T* xs = sm.dx[s];
+                const T* ys = sm.dy[s];
+                T cu = colv[s][q], rv = rowv[s][q];
+                for (int p = 0; p < m; ++p) {
+                    cu = fma(-xs[(size_t)j * ld + p], ys[(size_t)i * ld + p], cu);   // G_eff[j][i]
+                    rv = fma(-xs[(size_t)i * ld + p], ys[(size_t)j * ld + p], rv);   // G_eff[i][j]
+                }
+                sm.dx[s][(size_t)j * ld + m] = cu;
+                sm.dy[s][(size_t)j * ld + m] = ((j == i ? T(1) : T(0)) - rv) * a[s];
             }
         }
         if (threadIdx.x == 0) {
@@ -449,7 +621,21 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int sw, 
             ++*accepted;
         }
         __syncthreads();
+        if (++m == kd) {
+            GemmOpt<T> o;
+            o.subtract = true;
+            for (int s = 0; s < 2; ++s)
+                tile_gemm<T, false, true>(g[s], n, sm.dx[s], ld, sm.dy[s], ld, n, n, m, sm.stage, o);
+            m = 0;
+        }
     }
+    if (m > 0) {
+        GemmOpt<T> o;
+        o.subtract = true;
+        for (int s = 0; s < 2; ++s)
+            tile_gemm<T, false, true>(g[s], n, sm.dx[s], ld, sm.dy[s], ld, n, n, m, sm.stage, o);
+    }
+    __syncthreads();
 }
 
 template <typename T>
@@ -525,10 +711,12 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     __shared__ ChainDesc d;
     __shared__ int accepted;
     __shared__ int singular;
+    __shared__ long long sub[3];
     if (threadIdx.x == 0) {
         d = descs[blockIdx.x];
         accepted = 0;
         singular = 0;
+        sub[0] = sub[1] = sub[2] = 0;
     }
     __syncthreads();
     const int n = d.n;
@@ -544,6 +732,7 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     sm.s1 = sm.s0 + nn;
     sm.slots = w + lay.g_slots;
     sm.slot_bytes = lay.slot;
+    sm.sub = sub;
     double* p = smem;
     sm.sv = p; p += kNW + 8;
     sm.xv[0] = p; p += n;
@@ -565,7 +754,27 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     sm.yt[1] = tp; tp += n;
     p = reinterpret_cast<double*>(tp);
     p = smem + (((p - smem) + 3) & ~(ptrdiff_t)3);
+    sm.gii = p; p += 4;
     sm.stage = reinterpret_cast<T*>(p);
+    tp = sm.stage + tile_gemm_smem<T>() / sizeof(T);
+    const size_t dsz = (size_t)n * (d.delay + 1);
+    sm.dx[0] = tp; tp += dsz;
+    sm.dx[1] = tp; tp += dsz;
+    sm.dy[0] = tp; tp += dsz;
+    sm.dy[1] = tp; tp += dsz;
+    {
+        // LU panel over the delayed-update buffers (not in use during a refresh), then the
+        // pivot list and the float64 staging buffer
+        double* lp = reinterpret_cast<double*>(sm.dx[0]);
+        sm.panel = lp;
+        const size_t dbytes = 4 * dsz * sizeof(T);
+        const size_t pbytes = (size_t)n * (panel_width(n) + 1) * sizeof(double);
+        unsigned char* q = reinterpret_cast<unsigned char*>(lp) + (dbytes > pbytes ? dbytes : pbytes);
+        q = reinterpret_cast<unsigned char*>(((uintptr_t)q + 15) & ~(uintptr_t)15);
+        sm.piv = reinterpret_cast<int*>(q);
+        q += kPanel * sizeof(int);
+        sm.stage64 = reinterpret_cast<double*>(q);
+    }
 
     double max_resid = 0.0;
     double logdet[2] = {0.0, 0.0}, sgn[2] = {1.0, 1.0};
@@ -633,18 +842,31 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
         d.diag[6] = sgn[1];
         d.diag[7] += (double)n_sweeps;
         for (int k = 0; k < 5; ++k) d.diag[8 + k] = (double)ph[k];
+        for (int k = 0; k < 3; ++k) d.diag[13 + k] = (double)sub[k];
         if (singular) atomicOr(d.status, LQMC_STATUS_SINGULAR);
         if (max_resid > d.drift_tol) atomicOr(d.status, LQMC_STATUS_DRIFT);
     }
 }
 
 // bytes of dynamic shared memory / per-chain global work of the tiled kernel
-size_t sweep_tiled_smem_bytes(int n, bool fp32) {
+size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay) {
     size_t v = (size_t)(kNW + 8 + 9 * n);
     v = (v + 3) & ~(size_t)3;                                   // doubles
-    const size_t tvec = 6 * (size_t)n * (fp32 ? 4 : 8);         // T vectors, bytes
+    const size_t ts = fp32 ? 4 : 8;
+    const size_t tvec = 6 * (size_t)n * ts;                     // T vectors, bytes
     v += ((tvec + 7) / 8 + 3) & ~(size_t)3;
-    return v * sizeof(double) + (fp32 ? tile_gemm_smem<float>() : tile_gemm_smem<double>());
+    v += 4;                                                     // gii
+    const size_t dbytes = 4 * (size_t)n * (delay + 1) * ts;
+    const size_t pbytes = (size_t)n * (panel_width(n) + 1) * sizeof(double);
+    return v * sizeof(double) + (fp32 ? tile_gemm_smem<float>() : tile_gemm_smem<double>()) +
+           (dbytes > pbytes ? dbytes : pbytes) + 16 + kPanel * sizeof(int) + tile_gemm_smem<double>();
+}
+
+// largest delayed-update depth <= requested (0: 32 in fp32, 16 in fp64) that fits `cap`
+int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap) {
+    int k = requested > 0 ? requested : (fp32 ? 32 : 16);
+    while (k > 1 && sweep_tiled_smem_bytes(n, fp32, k) > cap) --k;
+    return k;
 }
 
 size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32) {
