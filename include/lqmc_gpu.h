@@ -49,6 +49,9 @@ extern "C" {
 /* precisions */
 #define LQMC_PREC_FP64 0     /* every floating-point operation in float64                */
 #define LQMC_PREC_MIXED 1    /* float32 G, wraps and delayed updates; FP64 stabilisation */
+#define LQMC_PREC_FP64E 2    /* float64 G and updates; every dense product a float64-accurate
+                                GEMM emulated on the BF16 tensor cores (49-bit sliced operands,
+                                exact FP32 accumulation); FP64 Householder QR                 */
 
 /* uniform-draw sources */
 #define LQMC_RNG_REPLAY 0    /* caller uploads the uniforms (e.g. numpy's stream)        */

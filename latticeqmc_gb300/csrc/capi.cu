@@ -16,10 +16,10 @@ namespace lqmc {
 size_t sweep_fp64_smem_bytes(int n, int flags);
 cudaError_t launch_sweep_fp64(const ChainDesc* d_descs, int n_chains, size_t smem, int n_sweeps,
                               int measure, cudaStream_t stream);
-size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay);
-int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap);
-size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32);
-cudaError_t launch_sweep_tiled(const ChainDesc* d_descs, int n_chains, size_t smem, bool fp32,
+size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu);
+int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap, bool emu);
+size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32, bool emu);
+cudaError_t launch_sweep_tiled(const ChainDesc* d_descs, int n_chains, size_t smem, int precision,
                                int n_sweeps, int measure, cudaStream_t stream);
 }  // namespace lqmc
 
@@ -31,7 +31,7 @@ constexpr int kMaxSitesSmem = 128;    // one-CTA shared-memory kernel (both mode
 constexpr int kMaxSitesTiled = 1024;  // tiled kernel (dqmc mode): 4 rows per thread
 
 // which sweep kernel runs a chain
-enum Kind : int { kSmemFp64 = 0, kTiledFp64 = 1, kTiledFp32 = 2 };
+enum Kind : int { kSmemFp64 = 0, kTiledFp64 = 1, kTiledFp32 = 2, kTiledFp64e = 3 };
 constexpr size_t kAlign = 32;   // doubles (256 bytes) between device sub-buffers
 
 std::string g_create_error;
@@ -143,7 +143,8 @@ int lqmc_create(const lqmc_params* params, lqmc_handle** out) {
     *out = nullptr;
     if (params->mode != LQMC_MODE_COMPAT && params->mode != LQMC_MODE_DQMC)
         return fail(nullptr, LQMC_ERR_INVALID, "unknown mode");
-    if (params->precision != LQMC_PREC_FP64 && params->precision != LQMC_PREC_MIXED)
+    if (params->precision != LQMC_PREC_FP64 && params->precision != LQMC_PREC_MIXED &&
+        params->precision != LQMC_PREC_FP64E)
         return fail(nullptr, LQMC_ERR_INVALID, "unknown precision");
     if (params->rng != LQMC_RNG_REPLAY && params->rng != LQMC_RNG_PHILOX)
         return fail(nullptr, LQMC_ERR_INVALID, "unknown rng");
@@ -155,8 +156,10 @@ int lqmc_create(const lqmc_params* params, lqmc_handle** out) {
         return fail(nullptr, LQMC_ERR_UNSUPPORTED, "compat mode runs on the shared-memory kernel only");
     if (params->stab_every < 0 || params->delay < 0)
         return fail(nullptr, LQMC_ERR_INVALID, "negative stab_every or delay");
-    if (params->precision == LQMC_PREC_MIXED && params->mode == LQMC_MODE_COMPAT)
+    if (params->precision != LQMC_PREC_FP64 && params->mode == LQMC_MODE_COMPAT)
         return fail(nullptr, LQMC_ERR_UNSUPPORTED, "compat mode replays float64 arithmetic only");
+    if (params->engine == LQMC_ENGINE_SMEM && params->precision == LQMC_PREC_FP64E)
+        return fail(nullptr, LQMC_ERR_UNSUPPORTED, "the shared-memory kernel has no emulated GEMM");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess) return fail(nullptr, LQMC_ERR_CUDA, std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e));
@@ -241,6 +244,7 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
         d.u = u[c];
         d.drift_tol = 1e-6;
         if (h->p.precision == LQMC_PREC_MIXED) kind[c] = kTiledFp32;
+        else if (h->p.precision == LQMC_PREC_FP64E) kind[c] = kTiledFp64e;
         else if (h->p.engine == LQMC_ENGINE_TILED) kind[c] = kTiledFp64;
         else kind[c] = (n <= kMaxSitesSmem) ? kSmemFp64 : kTiledFp64;
         if (kind[c] == kSmemFp64 && h->p.engine == LQMC_ENGINE_SMEM && n > kMaxSitesSmem) {
@@ -258,11 +262,11 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
             if (flags & lqmc::kGreenInGlobal) work += 2 * nn;
             if (flags & lqmc::kScratchInGlobal) work += 2 * nn;
         } else {
-            const bool f32 = kind[c] == kTiledFp32;
+            const bool f32 = kind[c] == kTiledFp32, emu = kind[c] == kTiledFp64e;
             d.flags = 0;
-            d.delay = lqmc::sweep_tiled_delay(n, f32, h->p.delay, smem_cap);
-            smem[c] = lqmc::sweep_tiled_smem_bytes(n, f32, d.delay);
-            work = (lqmc::sweep_tiled_work_bytes(n, d.n_chunks, f32) + 7) / 8;
+            d.delay = lqmc::sweep_tiled_delay(n, f32, h->p.delay, smem_cap, emu);
+            smem[c] = lqmc::sweep_tiled_smem_bytes(n, f32, d.delay, emu);
+            work = (lqmc::sweep_tiled_work_bytes(n, d.n_chunks, f32, emu) + 7) / 8;
             if (smem[c] > smem_cap) { release(h); return fail(h, LQMC_ERR_UNSUPPORTED, "lattice too large for shared memory"); }
         }
         const size_t fcopy = (kind[c] == kTiledFp32) ? 2 * round_up((nn + 1) / 2, kAlign) : 0;
@@ -503,8 +507,9 @@ int lqmc_sweep(lqmc_handle* h, int32_t n_sweeps, int32_t measure, void* stream_p
     auto launch = [&](Bucket& b, cudaStream_t st) {
         if (b.kind == kSmemFp64)
             return lqmc::launch_sweep_fp64(b.d_descs, (int)b.chains.size(), b.smem, n_sweeps, measure, st);
-        return lqmc::launch_sweep_tiled(b.d_descs, (int)b.chains.size(), b.smem, b.kind == kTiledFp32,
-                                        n_sweeps, measure, st);
+        const int prec = b.kind == kTiledFp32 ? 1 : (b.kind == kTiledFp64e ? 2 : 0);
+        return lqmc::launch_sweep_tiled(b.d_descs, (int)b.chains.size(), b.smem, prec, n_sweeps,
+                                        measure, st);
     };
     if (h->buckets.size() == 1) {
         LQMC_CK(h, launch(h->buckets[0], stream));

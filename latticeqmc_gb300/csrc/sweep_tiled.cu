@@ -18,6 +18,7 @@
 #include "block_gemm.cuh"
 #include "chain_desc.h"
 #include "lqmc_gpu.h"
+#include "ozaki_gemm.cuh"
 #include "philox.cuh"
 
 namespace lqmc {
@@ -30,13 +31,16 @@ __host__ __device__ constexpr size_t align256(size_t b) { return (b + 255) / 256
 // Per-chain global work layout of the tiled kernel (bytes from desc.work).
 template <typename T>
 struct TiledLayout {
-    size_t nn, g, z, s, slot, total;
-    __host__ __device__ TiledLayout(int n, int n_chunks) {
+    size_t nn, g, z, s, slot, total, oz, oz_ea;
+    __host__ __device__ TiledLayout(int n, int n_chunks, bool emu = false) {
         nn = (size_t)n * n;
         g = 0;                                              // G_up, G_dn          (T)
         z = g + align256(2 * nn * sizeof(T));               // Z0, Z1 GEMM temps   (T)
         s = z + align256(2 * nn * sizeof(T));               // S0, S1 QR / LU      (double)
-        const size_t slots = s + align256(2 * nn * sizeof(double));
+        oz = s + align256(2 * nn * sizeof(double));         // emulated GEMM slices (bf16)
+        const size_t oz_bytes = emu ? align256(ozk::slice_elems(n, n, n) * 2) : 0;
+        oz_ea = oz + oz_bytes;                              // emulated GEMM exponents (int)
+        const size_t slots = oz_ea + (emu ? align256(2 * (size_t)n * sizeof(int)) : 0);
         slot = align256(2 * nn * sizeof(T) + (size_t)(n + 1) * sizeof(double));
         total = slots + (size_t)(2 * n_chunks + 4) * slot;
         g_slots = slots;
@@ -70,6 +74,7 @@ struct TSmem {
     T* dy[2];     // Y_s (n x (kd + 1))
     double* gii;  // [2 parity][2 spins] diagonal of G_eff for the current site
     long long* sub;   // [3] clock cycles: Householder QR, Q and T formation, LU solve
+    ozk::Workspace oz;    // emulated float64 GEMM: slice buffers, exponents, staging
     double* panel;    // blocked LU panel, n x (kPanel + 1); aliases dx/dy (not live then)
     int* piv;         // [kPanel] panel pivots
     double* stage64;  // float64 GEMM staging of the LU
@@ -83,6 +88,19 @@ template <typename T> __device__ __forceinline__ T* slot_T(const TSmem<T>& sm, i
 }
 template <typename T> __device__ __forceinline__ double* slot_d(const TSmem<T>& sm, int idx, size_t nn) {
     return reinterpret_cast<double*>(slot_U(sm, idx, nn) + 2 * nn);
+}
+
+// Dense product of the tiled kernel: the block-tiled SIMT GEMM, or with EMU the float64
+// GEMM emulated on the BF16 tensor cores (ozaki_gemm.cuh).
+template <typename T, bool EMU, bool TA, bool TB, typename TAIn, typename TBIn>
+__device__ __forceinline__ void gemm_t(TSmem<T>& sm, T* c, int ldc, const TAIn* a, int lda,
+                                       const TBIn* b, int ldb, int m, int n, int k,
+                                       GemmOpt<T> o = GemmOpt<T>()) {
+    if constexpr (EMU) {
+        ozk::oz_gemm<TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.oz, o);
+    } else {
+        tile_gemm<T, TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.stage, o);
+    }
 }
 
 template <typename T> __device__ __forceinline__ const T* mat_expk(const ChainDesc& d);
@@ -163,9 +181,9 @@ constexpr int kPanel = 32;   // widest panel
 
 __host__ __device__ constexpr int panel_width(int n) { return n <= 256 ? 32 : (n <= 512 ? 16 : 8); }
 
-__device__ void lu_solve_blocked(double* w, double* rhs, int n, double* panel, int* piv,
-                                 double* stage, double* sv, double* logabs, double* sgn,
-                                 int* singular) {
+template <bool EMU>
+__device__ void lu_solve_blocked(TSmem<double>& sm, double* w, double* rhs, int n, double* panel,
+                                 int* piv, double* sv, double* logabs, double* sgn, int* singular) {
     const int lane = lane_id();
     const int P = panel_width(n), LD = P + 1;
     double la = 0.0, sg = 1.0;
@@ -251,11 +269,12 @@ __device__ void lu_solve_blocked(double* w, double* rhs, int n, double* panel, i
             GemmOpt<double> o;
             o.subtract = true;
             // W22 -= L21 U12 ; R2 -= L21 R1
-            tile_gemm<double, false, false>(w + (size_t)(jb + nb) * n + jb + nb, n,
-                                            w + (size_t)(jb + nb) * n + jb, n,
-                                            w + (size_t)jb * n + jb + nb, n, rest, rest, nb, stage, o);
-            tile_gemm<double, false, false>(rhs + (size_t)(jb + nb) * n, n, w + (size_t)(jb + nb) * n + jb, n,
-                                            rhs + (size_t)jb * n, n, rest, n, nb, stage, o);
+            gemm_t<double, EMU, false, false>(sm, w + (size_t)(jb + nb) * n + jb + nb, n,
+                                              w + (size_t)(jb + nb) * n + jb, n,
+                                              w + (size_t)jb * n + jb + nb, n, rest, rest, nb, o);
+            gemm_t<double, EMU, false, false>(sm, rhs + (size_t)(jb + nb) * n, n,
+                                              w + (size_t)(jb + nb) * n + jb, n,
+                                              rhs + (size_t)jb * n, n, rest, n, nb, o);
         }
     }
     // back substitution with U, 32-row blocks from the bottom
@@ -276,12 +295,35 @@ __device__ void lu_solve_blocked(double* w, double* rhs, int n, double* panel, i
             GemmOpt<double> o;
             o.subtract = true;
             // R0 -= U01 R1
-            tile_gemm<double, false, false>(rhs, n, w + jb, n, rhs + (size_t)jb * n, n, jb, n, nb, stage, o);
+            gemm_t<double, EMU, false, false>(sm, rhs, n, w + jb, n, rhs + (size_t)jb * n, n, jb, n, nb, o);
         }
     }
     *logabs = la;
     *sgn = sg;
     *singular = sing;
+}
+
+// The LU of the stabilised inverse works in float64 on S0 / S1.  With T = double its
+// trailing updates use the kernel's GEMM (tiled or emulated); with T = float they use a
+// float64 tiled GEMM on the separate float64 staging buffer.
+template <typename T, bool EMU>
+__device__ void lu_solve_dispatch(TSmem<T>& sm, int n, double* la, double* sw, int* sing);
+
+template <>
+__device__ void lu_solve_dispatch<double, false>(TSmem<double>& sm, int n, double* la, double* sw, int* sing) {
+    lu_solve_blocked<false>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
+}
+template <>
+__device__ void lu_solve_dispatch<double, true>(TSmem<double>& sm, int n, double* la, double* sw, int* sing) {
+    lu_solve_blocked<true>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
+}
+template <>
+__device__ void lu_solve_dispatch<float, false>(TSmem<float>& sm, int n, double* la, double* sw, int* sing) {
+    // a float64 view of the workspace pointers for the float64 LU
+    TSmem<double> d;
+    d.stage = sm.stage64;
+    d.oz = sm.oz;
+    lu_solve_blocked<false>(d, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
 }
 
 // Q = H_0 ... H_{n-2} in precision T, column-major (qc[k n + i] = Q[i][k]), from the
@@ -378,7 +420,7 @@ __device__ double udt_absorb_t(const ChainDesc& d, TSmem<T>& sm, const T* z, con
 
 // G = (1 + U_R D_R T_R T_L^T D_L U_L^T)^-1; ul == nullptr: identity left product.
 // U_R, U_L column-major (uc[k n + i] = U[i][k]), T_R, T_L row-major.
-template <typename T>
+template <typename T, bool EMU>
 __device__ double green_udt_t(const ChainDesc& d, TSmem<T>& sm, const T* ur, const double* dr,
                               const T* tr, double sign_r, const T* ul, const double* dl,
                               const T* tl, double sign_l, T* g, bool residual, double* logdet,
@@ -403,8 +445,8 @@ __device__ double green_udt_t(const ChainDesc& d, TSmem<T>& sm, const T* ur, con
     }
     if (ul) {
         // X = U_R^T U_L: A(i,p) = U_R[p][i] = ur[i n + p]; B(p,j) = U_L[p][j] = ul[j n + p]
-        tile_gemm<T, false, true>(sm.z0, n, ur, n, ul, n, n, n, n, sm.stage);
-        tile_gemm<T, false, true>(sm.z1, n, tr, n, tl, n, n, n, n, sm.stage);   // Y = T_R T_L^T
+        gemm_t<T, EMU, false, true>(sm, sm.z0, n, ur, n, ul, n, n, n, n);
+        gemm_t<T, EMU, false, true>(sm, sm.z1, n, tr, n, tl, n, n, n, n);   // Y = T_R T_L^T
     }
     __syncthreads();
     for (int i = warp_id(); i < n; i += kNW)
@@ -419,7 +461,7 @@ __device__ double green_udt_t(const ChainDesc& d, TSmem<T>& sm, const T* ur, con
     double la, sw;
     int sing;
     const long long t0 = clock64();
-    lu_solve_blocked(sm.s0, sm.s1, n, sm.panel, sm.piv, sm.stage64, sm.sv, &la, &sw, &sing);
+    lu_solve_dispatch<T, EMU>(sm, n, &la, &sw, &sing);
     if (threadIdx.x == 0) sm.sub[2] += clock64() - t0;
     if (sing) *singular = 1;
     double res = 0.0, m = 0.0;
@@ -428,7 +470,7 @@ __device__ double green_udt_t(const ChainDesc& d, TSmem<T>& sm, const T* ur, con
             for (int j = lane; j < n; j += 32) sm.s1[(size_t)i * n + j] /= dbl[i];
         __syncthreads();
         // G = U_L Z: A(i,p) = U_L[i][p] = ul[p n + i]
-        tile_gemm<T, true, false>(sm.z0, n, ul, n, sm.s1, n, n, n, n, sm.stage);
+        gemm_t<T, EMU, true, false>(sm, sm.z0, n, ul, n, sm.s1, n, n, n, n);
         for (int i = warp_id(); i < n; i += kNW)
             for (int j = lane; j < n; j += 32) {
                 const size_t e = (size_t)i * n + j;
@@ -453,7 +495,7 @@ __device__ double green_udt_t(const ChainDesc& d, TSmem<T>& sm, const T* ur, con
     return res;
 }
 
-template <typename T>
+template <typename T, bool EMU>
 __device__ void right_stack_t(const ChainDesc& d, TSmem<T>& sm, int s, double* logdet, double* sgn,
                               int* singular) {
     const int n = d.n, sigma = s ? -1 : 1;
@@ -477,9 +519,9 @@ __device__ void right_stack_t(const ChainDesc& d, TSmem<T>& sm, int s, double* l
                 __syncthreads();
             } else if (l == lo) {
                 // B(p, j) = U[p][j] = uc[j n + p] (column-major slot)
-                tile_gemm<T, false, true>(zb, n, ek, n, slot_U(sm, prev, nn), n, n, n, n, sm.stage, o);
+                gemm_t<T, EMU, false, true>(sm, zb, n, ek, n, slot_U(sm, prev, nn), n, n, n, n, o);
             } else {
-                tile_gemm<T, false, false>(zb, n, ek, n, za, n, n, n, n, sm.stage, o);   // e^V e^{-dtau K} Z
+                gemm_t<T, EMU, false, false>(sm, zb, n, ek, n, za, n, n, n, n, o);   // e^V e^{-dtau K} Z
             }
             T* t = za; za = zb; zb = t;
         }
@@ -490,12 +532,12 @@ __device__ void right_stack_t(const ChainDesc& d, TSmem<T>& sm, int s, double* l
         __syncthreads();
     }
     const int top = s * d.n_chunks + d.n_chunks - 1;
-    green_udt_t<T>(d, sm, slot_U(sm, top, nn), slot_d(sm, top, nn), slot_T(sm, top, nn),
+    green_udt_t<T, EMU>(d, sm, slot_U(sm, top, nn), slot_d(sm, top, nn), slot_T(sm, top, nn),
                    slot_d(sm, top, nn)[n], nullptr, nullptr, nullptr, 1.0, sm.g[s], false, logdet,
                    sgn, singular);
 }
 
-template <typename T>
+template <typename T, bool EMU>
 __device__ void left_step_t(const ChainDesc& d, TSmem<T>& sm, int s, int p_in, bool first, int lo,
                             int hi) {
     const int n = d.n, sigma = s ? -1 : 1;
@@ -520,7 +562,7 @@ __device__ void left_step_t(const ChainDesc& d, TSmem<T>& sm, int s, int p_in, b
                 for (int j = lane; j < n; j += 32)
                     za[(size_t)i * n + j] = sm.ev_t[i] * za[(size_t)i * n + j];
         }
-        tile_gemm<T, true, false>(zb, n, ek, n, za, n, n, n, n, sm.stage);   // e^{-dtau K}^T (e^V Z)
+        gemm_t<T, EMU, true, false>(sm, zb, n, ek, n, za, n, n, n, n);   // e^{-dtau K}^T (e^V Z)
         T* t = za; za = zb; zb = t;
     }
     const double sg = udt_absorb_t<T>(d, sm, za, first ? nullptr : slot_d(sm, in, nn),
@@ -530,7 +572,7 @@ __device__ void left_step_t(const ChainDesc& d, TSmem<T>& sm, int s, int p_in, b
     __syncthreads();
 }
 
-template <typename T>
+template <typename T, bool EMU>
 __device__ void wrap_t(const ChainDesc& d, TSmem<T>& sm, int l) {
     const int n = d.n;
     const size_t nn = (size_t)n * n;
@@ -542,8 +584,8 @@ __device__ void wrap_t(const ChainDesc& d, TSmem<T>& sm, int l) {
             for (int j = lane_id(); j < n; j += 32) g[(size_t)i * n + j] *= sm.iev_t[i];
         GemmOpt<T> o;
         o.cs = sm.ev_t;
-        tile_gemm<T, false, false>(sm.z0, n, mat_expkinv<T>(d), n, g, n, n, n, n, sm.stage, o);
-        tile_gemm<T, false, false>(g, n, sm.z0, n, mat_expk<T>(d), n, n, n, n, sm.stage);
+        gemm_t<T, EMU, false, false>(sm, sm.z0, n, mat_expkinv<T>(d), n, g, n, n, n, n, o);
+        gemm_t<T, EMU, false, false>(sm, g, n, sm.z0, n, mat_expk<T>(d), n, n, n, n);
     }
 }
 
@@ -551,7 +593,7 @@ __device__ void wrap_t(const ChainDesc& d, TSmem<T>& sm, int l) {
 // the slice accumulate as G_eff = G - X Y^T with x = G_eff[:, i], y = (D/R)(e_i - G_eff[i, :])
 // (the Sherman-Morrison update of lqmc.py:318-331 with the defects fixed); every k flips,
 // and at the end of the slice, G -= X Y^T as one tiled GEMM per spin.
-template <typename T>
+template <typename T, bool EMU>
 __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int sw, uint64_t sweep_id,
                                int* accepted) {
     const int n = d.n, L = d.L, step = L - 1 - l, kd = d.delay, ld = kd + 1;
@@ -625,7 +667,7 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int sw, 
             GemmOpt<T> o;
             o.subtract = true;
             for (int s = 0; s < 2; ++s)
-                tile_gemm<T, false, true>(g[s], n, sm.dx[s], ld, sm.dy[s], ld, n, n, m, sm.stage, o);
+                gemm_t<T, EMU, false, true>(sm, g[s], n, sm.dx[s], ld, sm.dy[s], ld, n, n, m, o);
             m = 0;
         }
     }
@@ -633,7 +675,7 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int sw, 
         GemmOpt<T> o;
         o.subtract = true;
         for (int s = 0; s < 2; ++s)
-            tile_gemm<T, false, true>(g[s], n, sm.dx[s], ld, sm.dy[s], ld, n, n, m, sm.stage, o);
+            gemm_t<T, EMU, false, true>(sm, g[s], n, sm.dx[s], ld, sm.dy[s], ld, n, n, m, o);
     }
     __syncthreads();
 }
@@ -704,7 +746,7 @@ __device__ void measure_t(const ChainDesc& d, TSmem<T>& sm) {
 
 }  // namespace
 
-template <typename T>
+template <typename T, bool EMU>
 __global__ void __launch_bounds__(kNT, 1)
 sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_measure) {
     extern __shared__ __align__(16) double smem[];
@@ -721,7 +763,7 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     __syncthreads();
     const int n = d.n;
     const size_t nn = (size_t)n * n;
-    TiledLayout<T> lay(n, d.n_chunks);
+    TiledLayout<T> lay(n, d.n_chunks, EMU);
     unsigned char* w = reinterpret_cast<unsigned char*>(d.work);
     TSmem<T> sm;
     sm.g[0] = reinterpret_cast<T*>(w + lay.g);
@@ -756,7 +798,13 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     p = smem + (((p - smem) + 3) & ~(ptrdiff_t)3);
     sm.gii = p; p += 4;
     sm.stage = reinterpret_cast<T*>(p);
-    tp = sm.stage + tile_gemm_smem<T>() / sizeof(T);
+    sm.oz.stage = reinterpret_cast<unsigned char*>(p);
+    constexpr size_t stage_region = (EMU && ozk::stage_bytes() > tile_gemm_smem<T>())
+                                        ? ozk::stage_bytes() : tile_gemm_smem<T>();
+    tp = sm.stage + stage_region / sizeof(T);
+    sm.oz.slices = reinterpret_cast<__nv_bfloat16*>(w + lay.oz);
+    sm.oz.ea = reinterpret_cast<int*>(w + lay.oz_ea);
+    sm.oz.eb = sm.oz.ea + n;
     const size_t dsz = (size_t)n * (d.delay + 1);
     sm.dx[0] = tp; tp += dsz;
     sm.dx[1] = tp; tp += dsz;
@@ -789,24 +837,24 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
         tc = t_;                            \
     } while (0)
     for (int sw = 0; sw < n_sweeps; ++sw, ++sweep_id) {
-        right_stack_t<T>(d, sm, 0, &logdet[0], &sgn[0], &singular);
-        right_stack_t<T>(d, sm, 1, &logdet[1], &sgn[1], &singular);
+        right_stack_t<T, EMU>(d, sm, 0, &logdet[0], &sgn[0], &singular);
+        right_stack_t<T, EMU>(d, sm, 1, &logdet[1], &sgn[1], &singular);
         LQMC_PHASE(0);
         int lp[2] = {0, 0};
         for (int c = d.n_chunks - 1; c >= 0; --c) {
             const int lo = c * d.stab_every, hi = min(lo + d.stab_every, d.L);
             for (int l = hi - 1; l >= lo; --l) {
-                update_slice_t<T>(d, sm, l, sw, sweep_id, &accepted);
+                update_slice_t<T, EMU>(d, sm, l, sw, sweep_id, &accepted);
                 LQMC_PHASE(1);
-                if (l > 0) wrap_t<T>(d, sm, l);
+                if (l > 0) wrap_t<T, EMU>(d, sm, l);
                 LQMC_PHASE(2);
             }
             if (c > 0) {
                 for (int s = 0; s < 2; ++s) {
-                    left_step_t<T>(d, sm, s, lp[s], c == d.n_chunks - 1, lo, hi);
+                    left_step_t<T, EMU>(d, sm, s, lp[s], c == d.n_chunks - 1, lo, hi);
                     lp[s] ^= 1;
                     const int rs = s * d.n_chunks + c - 1, ls = 2 * d.n_chunks + 2 * s + lp[s];
-                    const double r = green_udt_t<T>(
+                    const double r = green_udt_t<T, EMU>(
                         d, sm, slot_U(sm, rs, nn), slot_d(sm, rs, nn), slot_T(sm, rs, nn),
                         slot_d(sm, rs, nn)[n], slot_U(sm, ls, nn), slot_d(sm, ls, nn),
                         slot_T(sm, ls, nn), slot_d(sm, ls, nn)[n], sm.g[s], true, &logdet[s],
@@ -849,7 +897,7 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
 }
 
 // bytes of dynamic shared memory / per-chain global work of the tiled kernel
-size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay) {
+size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu) {
     size_t v = (size_t)(kNW + 8 + 9 * n);
     v = (v + 3) & ~(size_t)3;                                   // doubles
     const size_t ts = fp32 ? 4 : 8;
@@ -858,39 +906,41 @@ size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay) {
     v += 4;                                                     // gii
     const size_t dbytes = 4 * (size_t)n * (delay + 1) * ts;
     const size_t pbytes = (size_t)n * (panel_width(n) + 1) * sizeof(double);
-    return v * sizeof(double) + (fp32 ? tile_gemm_smem<float>() : tile_gemm_smem<double>()) +
-           (dbytes > pbytes ? dbytes : pbytes) + 16 + kPanel * sizeof(int) + tile_gemm_smem<double>();
+    size_t stage = fp32 ? tile_gemm_smem<float>() : tile_gemm_smem<double>();
+    if (emu && ozk::stage_bytes() > stage) stage = ozk::stage_bytes();
+    return v * sizeof(double) + stage + (dbytes > pbytes ? dbytes : pbytes) + 16 +
+           kPanel * sizeof(int) + tile_gemm_smem<double>();
 }
 
 // largest delayed-update depth <= requested (0: 32 in fp32, 16 in fp64) that fits `cap`
-int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap) {
+int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap, bool emu) {
     int k = requested > 0 ? requested : (fp32 ? 32 : 16);
-    while (k > 1 && sweep_tiled_smem_bytes(n, fp32, k) > cap) --k;
+    while (k > 1 && sweep_tiled_smem_bytes(n, fp32, k, emu) > cap) --k;
     return k;
 }
 
-size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32) {
-    return fp32 ? TiledLayout<float>(n, n_chunks).total : TiledLayout<double>(n, n_chunks).total;
+size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32, bool emu) {
+    return fp32 ? TiledLayout<float>(n, n_chunks).total : TiledLayout<double>(n, n_chunks, emu).total;
 }
 
-cudaError_t launch_sweep_tiled(const ChainDesc* d_descs, int n_chains, size_t smem, bool fp32,
-                               int n_sweeps, int measure, cudaStream_t stream) {
-    if (fp32) {
-        if (smem > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(sweep_tiled_kernel<float>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-        }
-        sweep_tiled_kernel<float><<<n_chains, kNT, smem, stream>>>(d_descs, n_sweeps, measure);
-    } else {
-        if (smem > 48 * 1024) {
-            cudaError_t e = cudaFuncSetAttribute(sweep_tiled_kernel<double>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-        }
-        sweep_tiled_kernel<double><<<n_chains, kNT, smem, stream>>>(d_descs, n_sweeps, measure);
+template <typename T, bool EMU>
+static cudaError_t launch_tiled(const ChainDesc* d_descs, int n_chains, size_t smem, int n_sweeps,
+                                int measure, cudaStream_t stream) {
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(sweep_tiled_kernel<T, EMU>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
     }
+    sweep_tiled_kernel<T, EMU><<<n_chains, kNT, smem, stream>>>(d_descs, n_sweeps, measure);
     return cudaGetLastError();
+}
+
+// precision: 0 float64, 1 float32 (mixed), 2 float64 with emulated tensor-core GEMMs
+cudaError_t launch_sweep_tiled(const ChainDesc* d_descs, int n_chains, size_t smem, int precision,
+                               int n_sweeps, int measure, cudaStream_t stream) {
+    if (precision == 1) return launch_tiled<float, false>(d_descs, n_chains, smem, n_sweeps, measure, stream);
+    if (precision == 2) return launch_tiled<double, true>(d_descs, n_chains, smem, n_sweeps, measure, stream);
+    return launch_tiled<double, false>(d_descs, n_chains, smem, n_sweeps, measure, stream);
 }
 
 }  // namespace lqmc

@@ -74,8 +74,9 @@ class Engine:
 
     mode       'compat' (reference arithmetic, lqmc/lqmc.py:301-347) or 'dqmc' (textbook,
                stabilised)
-    precision  'fp64', or 'mixed' (float32 G, wraps, updates and B-chain products; float64
-               Householder QR and LU of the stabilisation)
+    precision  'fp64'; 'fp64e' (float64 G and updates, every dense product a float64-accurate
+               GEMM emulated on the BF16 tensor cores); or 'mixed' (float32 G, wraps, updates
+               and B-chain products; float64 Householder QR and LU of the stabilisation)
     rng        'replay' (uniforms uploaded per sweep) or 'philox' (on device)
     engine     'auto', 'smem' (one CTA per chain, G in shared memory, fp64, N <= 128) or
                'tiled' (matrices in global memory, tiled GEMMs; any N up to 2048)

@@ -107,3 +107,46 @@ def test_mixed_precision_2x2_observables_match_exact_diagonalisation():
         vals = np.array([o[key] for o in obs])
         mean, err = vals.mean(), vals.std(ddof=1) / np.sqrt(n_chains)
         assert abs(mean - ref) < 4 * err + 1e-4, f"{key}: {mean:.5f} +- {err:.5f} vs ED {ref:.5f}"
+
+
+@pytest.mark.parametrize("side,beta,L,stab", [(4, 4.0, 40, 5), (8, 4.0, 80, 10), (12, 4.0, 40, 5)])
+def test_fp64e_matches_oracle(side, beta, L, stab):
+    """Every dense product on the BF16 tensor cores with 48-bit sliced operands: decisions
+    as the float64 oracle, G within the wrap-amplified truncation error (1e-8)."""
+    K, field, rng = _setup(side, beta, L, 500 + side)
+    N = side * side
+    spec = ChainSpec(K, 4.0, beta, L, field)
+    ch = odqmc.Chain(spec.exp_k, expm(spec.dtau * K), spec.lamb, field, stab)
+    eng = Engine([spec], mode="dqmc", precision="fp64e", rng="replay", record=True, stab_every=stab)
+    for sw in range(2 if N <= 64 else 1):
+        u = rng.random(N * L)
+        rec = {}
+        g_or = ch.sweep(u, record=rec)
+        eng.set_uniforms(0, u)
+        eng.sweep(1)
+        assert np.array_equal(eng.decisions(0)[0], rec["accept"])
+        dg = np.abs(eng.green(0) - g_or).max()
+        print(f"fp64e vs oracle {side}x{side}: max|dG| {dg:.2e}")
+        assert dg < 1e-8
+    assert not eng.status().any()
+    eng.close()
+
+
+def test_fp64e_against_fp64_engine_16x16_beta8():
+    """The headline configuration's lattice: identical inputs, one sweep, max|dG| <= 1e-6."""
+    K, field, rng = _setup(16, 8.0, 80, 16)
+    spec = ChainSpec(K, 4.0, 8.0, 80, field)
+    a = Engine([spec], mode="dqmc", precision="fp64", rng="replay", stab_every=8, record=True)
+    b = Engine([spec], mode="dqmc", precision="fp64e", rng="replay", stab_every=8, record=True)
+    u = rng.random(256 * 80)
+    a.set_uniforms(0, u)
+    b.set_uniforms(0, u)
+    a.sweep(1)
+    b.sweep(1)
+    assert np.array_equal(a.decisions(0), b.decisions(0))
+    dg = np.abs(a.green(0) - b.green(0)).max()
+    print(f"fp64e vs fp64 16x16 beta=8: max|dG| {dg:.2e}, residual {b.diagnostics(0)['max_residual']:.1e}")
+    assert dg < 1e-6
+    assert not (b.status() & 3).any()
+    a.close()
+    b.close()
