@@ -1,6 +1,10 @@
-// Persistent dqmc sweep kernel for large lattices and for mixed precision: one CTA per
-// Markov chain, every n x n matrix in global memory (L2-resident for tens of chains at
-// N = 256), dense products through the block-tiled GEMM of block_gemm.cuh.
+// Persistent dqmc sweep kernel for large lattices and for mixed precision: a cluster of two
+// CTAs per Markov chain, one per spin, every n x n matrix in global memory (L2-resident for
+// tens of chains at N = 256), dense products through the block-tiled GEMM of
+// block_gemm.cuh or the emulated float64 GEMM of ozaki_gemm.cuh.  The spins only meet in
+// the acceptance ratio R = R_up R_dn of each site, whose two factors the CTAs exchange
+// through distributed shared memory under one cluster barrier per site, and in the
+// measurements.
 //
 // Template parameter T is the precision of G, of the wraps, of the rank-1 updates and of
 // the B-chain products (float: the mixed-precision engine; double: the plain FP64 engine).
@@ -11,6 +15,7 @@
 //   G' = G - (D/R) G[:, i] (e_i - G[i, :])                 rank-1 update
 //   G <- e^{+dtau K} e^{-V_l} G e^{V_l} e^{-dtau K}         wrap from slice l to l-1
 //   refresh every stab_every slices from the UDT right stack and left product.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -28,29 +33,33 @@ using namespace blk;
 
 __host__ __device__ constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 
-// Per-chain global work layout of the tiled kernel (bytes from desc.work).
+// Per-chain global work layout of the tiled kernel (bytes from desc.work): one block per
+// spin (its CTA's G, GEMM temporaries, float64 QR / LU buffers, emulated-GEMM slices), then
+// the UDT slots of both spins.
 template <typename T>
 struct TiledLayout {
-    size_t nn, g, z, s, slot, total, oz, oz_ea;
+    size_t nn, g, z, s, oz, oz_ea, spin_block, slot, total, g_slots;
     __host__ __device__ TiledLayout(int n, int n_chunks, bool emu = false) {
         nn = (size_t)n * n;
-        g = 0;                                              // G_up, G_dn          (T)
-        z = g + align256(2 * nn * sizeof(T));               // Z0, Z1 GEMM temps   (T)
+        g = 0;                                              // G of the spin       (T)
+        z = g + align256(nn * sizeof(T));                   // Z0, Z1 GEMM temps   (T)
         s = z + align256(2 * nn * sizeof(T));               // S0, S1 QR / LU      (double)
         oz = s + align256(2 * nn * sizeof(double));         // emulated GEMM slices (bf16)
         const size_t oz_bytes = emu ? align256(ozk::slice_elems(n, n, n) * 2) : 0;
         oz_ea = oz + oz_bytes;                              // emulated GEMM exponents (int)
-        const size_t slots = oz_ea + (emu ? align256(2 * (size_t)n * sizeof(int)) : 0);
+        spin_block = oz_ea + (emu ? align256(2 * (size_t)n * sizeof(int)) : 0);
+        g_slots = 2 * spin_block;
         slot = align256(2 * nn * sizeof(T) + (size_t)(n + 1) * sizeof(double));
-        total = slots + (size_t)(2 * n_chunks + 4) * slot;
-        g_slots = slots;
+        total = g_slots + (size_t)(2 * n_chunks + 4) * slot;
     }
-    size_t g_slots;
 };
 
 template <typename T>
 struct TSmem {
-    T* g[2];
+    int spin;         // the spin this CTA owns (its cluster rank)
+    T* g;             // G of that spin
+    double* peer_gii; // the partner CTA's gii buffer (distributed shared memory)
+    double* peer_xv;  // the partner CTA's xv[0] (its xv[1] follows)
     T* z0;
     T* z1;
     double* s0;
@@ -70,9 +79,9 @@ struct TSmem {
     T* xt[2];     // rank-1 update vectors in precision T
     T* yt[2];
     T* stage;
-    T* dx[2];     // delayed updates: X_s (n x (kd + 1)), G_eff = G - X Y^T
-    T* dy[2];     // Y_s (n x (kd + 1))
-    double* gii;  // [2 parity][2 spins] diagonal of G_eff for the current site
+    T* dx;        // delayed updates: X (n x (kd + 1)), G_eff = G - X Y^T
+    T* dy;        // Y (n x (kd + 1))
+    double* gii;  // [2 parity][2 spins] diagonal of G_eff for the current site, both spins
     long long* sub;   // [3] clock cycles: Householder QR, Q and T formation, LU solve
     ozk::Workspace oz;    // emulated float64 GEMM: slice buffers, exponents, staging
     double* panel;    // blocked LU panel, n x (kPanel + 1); aliases dx/dy (not live then)
@@ -533,7 +542,7 @@ __device__ void right_stack_t(const ChainDesc& d, TSmem<T>& sm, int s, double* l
     }
     const int top = s * d.n_chunks + d.n_chunks - 1;
     green_udt_t<T, EMU>(d, sm, slot_U(sm, top, nn), slot_d(sm, top, nn), slot_T(sm, top, nn),
-                   slot_d(sm, top, nn)[n], nullptr, nullptr, nullptr, 1.0, sm.g[s], false, logdet,
+                   slot_d(sm, top, nn)[n], nullptr, nullptr, nullptr, 1.0, sm.g, false, logdet,
                    sgn, singular);
 }
 
@@ -575,18 +584,15 @@ __device__ void left_step_t(const ChainDesc& d, TSmem<T>& sm, int s, int p_in, b
 template <typename T, bool EMU>
 __device__ void wrap_t(const ChainDesc& d, TSmem<T>& sm, int l) {
     const int n = d.n;
-    const size_t nn = (size_t)n * n;
-    for (int s = 0; s < 2; ++s) {
-        load_ev_t<T>(d, sm, l, s ? -1 : 1);
-        __syncthreads();
-        T* g = sm.g[s];
-        for (int i = warp_id(); i < n; i += kNW)
-            for (int j = lane_id(); j < n; j += 32) g[(size_t)i * n + j] *= sm.iev_t[i];
-        GemmOpt<T> o;
-        o.cs = sm.ev_t;
-        gemm_t<T, EMU, false, false>(sm, sm.z0, n, mat_expkinv<T>(d), n, g, n, n, n, n, o);
-        gemm_t<T, EMU, false, false>(sm, g, n, sm.z0, n, mat_expk<T>(d), n, n, n, n);
-    }
+    load_ev_t<T>(d, sm, l, sm.spin ? -1 : 1);
+    __syncthreads();
+    T* g = sm.g;
+    for (int i = warp_id(); i < n; i += kNW)
+        for (int j = lane_id(); j < n; j += 32) g[(size_t)i * n + j] *= sm.iev_t[i];
+    GemmOpt<T> o;
+    o.cs = sm.ev_t;
+    gemm_t<T, EMU, false, false>(sm, sm.z0, n, mat_expkinv<T>(d), n, g, n, n, n, n, o);
+    gemm_t<T, EMU, false, false>(sm, g, n, sm.z0, n, mat_expk<T>(d), n, n, n, n);
 }
 
 // Site updates of slice l with delayed rank-k updates (k = d.delay): the accepted flips of
@@ -596,181 +602,186 @@ __device__ void wrap_t(const ChainDesc& d, TSmem<T>& sm, int l) {
 template <typename T, bool EMU>
 __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int sw, uint64_t sweep_id,
                                int* accepted) {
-    const int n = d.n, L = d.L, step = L - 1 - l, kd = d.delay, ld = kd + 1;
-    T* g[2] = {sm.g[0], sm.g[1]};
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int n = d.n, L = d.L, step = L - 1 - l, kd = d.delay, ld = kd + 1, sp = sm.spin;
+    T* g = sm.g;
     int8_t* f = d.field + (size_t)l * n;
     int m = 0;   // pending updates
     constexpr int kPer = 4;   // rows per thread: n <= kPer * kNT
     for (int i = 0; i < n; ++i) {
-        // G[:, i] and G[i, :] of both spins, loaded before they are needed
-        T colv[2][kPer], rowv[2][kPer];
+        // G[:, i] and G[i, :] of this spin, loaded before they are needed
+        T colv[kPer], rowv[kPer];
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
             const int j = threadIdx.x + q * kNT;
-#pragma unroll
-            for (int s = 0; s < 2; ++s) {
-                colv[s][q] = (j < n) ? g[s][(size_t)j * n + i] : T(0);
-                rowv[s][q] = (j < n) ? g[s][(size_t)i * n + j] : T(0);
-            }
+            colv[q] = (j < n) ? g[(size_t)j * n + i] : T(0);
+            rowv[q] = (j < n) ? g[(size_t)i * n + j] : T(0);
         }
-        double* gii = sm.gii + 2 * (i & 1);
+        // read the field before the barrier: after it either CTA may flip it
+        const int8_t s_il = f[i];
+        const int par = 2 * (i & 1);
         if (warp_id() == 0) {
             const int lane = lane_id();
+            T part = T(0);
+            for (int q = lane; q < m; q += 32) part = fma(sm.dx[(size_t)i * ld + q], sm.dy[(size_t)i * ld + q], part);
 #pragma unroll
-            for (int s = 0; s < 2; ++s) {
-                T part = T(0);
-                for (int q = lane; q < m; q += 32) part = fma(sm.dx[s][(size_t)i * ld + q], sm.dy[s][(size_t)i * ld + q], part);
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-                if (lane == 0) gii[s] = (double)(g[s][(size_t)i * n + i] - part);
+            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+            if (lane == 0) {
+                const double gv = (double)(g[(size_t)i * n + i] - part);
+                sm.gii[par + sp] = gv;
+                sm.peer_gii[par + sp] = gv;
             }
         }
-        __syncthreads();
+        cluster.sync();
         const int pos = step * n + i;
-        const int8_t s_il = f[i];
         double u;
         if (d.rng == LQMC_RNG_REPLAY) u = d.uniforms[(size_t)sw * n * L + pos];
         else u = philox_uniform(d.seed, (uint64_t)d.chain_id, sweep_id, (uint64_t)pos);
-        const double gi0 = gii[0], gi1 = gii[1];
+        const double gi0 = sm.gii[par], gi1 = sm.gii[par + 1];
         const double ep = s_il > 0 ? d.c[0] : d.c[1];
         const double em = s_il > 0 ? d.c[1] : d.c[0];
         const double dl_up = ep - 1.0, dl_dn = em - 1.0;
         const double r_up = 1.0 + dl_up * (1.0 - gi0), r_dn = 1.0 + dl_dn * (1.0 - gi1);
         const double ratio = r_up * r_dn;
         const bool acc = (u <= ratio);
-        if (d.record && threadIdx.x == 0) d.decisions[((size_t)sw * L + step) * n + i] = acc ? 1 : 0;
+        if (sp == 0 && d.record && threadIdx.x == 0) d.decisions[((size_t)sw * L + step) * n + i] = acc ? 1 : 0;
         if (!acc) continue;
-        const T a[2] = {(T)(dl_up / r_up), (T)(dl_dn / r_dn)};
+        const T a = sp ? (T)(dl_dn / r_dn) : (T)(dl_up / r_up);
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
             const int j = threadIdx.x + q * kNT;
             if (j >= n) break;
-#pragma unroll
-            for (int s = 0; s < 2; ++s) {
-                const T* xs = sm.dx[s];
-                const T* ys = sm.dy[s];
-                T cu = colv[s][q], rv = rowv[s][q];
-                for (int p = 0; p < m; ++p) {
-                    cu = fma(-xs[(size_t)j * ld + p], ys[(size_t)i * ld + p], cu);   // G_eff[j][i]
-                    rv = fma(-xs[(size_t)i * ld + p], ys[(size_t)j * ld + p], rv);   // G_eff[i][j]
-                }
-                sm.dx[s][(size_t)j * ld + m] = cu;
-                sm.dy[s][(size_t)j * ld + m] = ((j == i ? T(1) : T(0)) - rv) * a[s];
+            T cu = colv[q], rv = rowv[q];
+            for (int p = 0; p < m; ++p) {
+                cu = fma(-sm.dx[(size_t)j * ld + p], sm.dy[(size_t)i * ld + p], cu);   // G_eff[j][i]
+                rv = fma(-sm.dx[(size_t)i * ld + p], sm.dy[(size_t)j * ld + p], rv);   // G_eff[i][j]
             }
+            sm.dx[(size_t)j * ld + m] = cu;
+            sm.dy[(size_t)j * ld + m] = ((j == i ? T(1) : T(0)) - rv) * a;
         }
         if (threadIdx.x == 0) {
-            f[i] = (int8_t)(-s_il);
-            ++*accepted;
+            f[i] = (int8_t)(-s_il);   // both CTAs write the same value
+            if (sp == 0) ++*accepted;
         }
         __syncthreads();
         if (++m == kd) {
             GemmOpt<T> o;
             o.subtract = true;
-            for (int s = 0; s < 2; ++s)
-                gemm_t<T, EMU, false, true>(sm, g[s], n, sm.dx[s], ld, sm.dy[s], ld, n, n, m, o);
+            gemm_t<T, EMU, false, true>(sm, g, n, sm.dx, ld, sm.dy, ld, n, n, m, o);
             m = 0;
         }
     }
     if (m > 0) {
         GemmOpt<T> o;
         o.subtract = true;
-        for (int s = 0; s < 2; ++s)
-            gemm_t<T, EMU, false, true>(sm, g[s], n, sm.dx[s], ld, sm.dy[s], ld, n, n, m, o);
+        gemm_t<T, EMU, false, true>(sm, g, n, sm.dx, ld, sm.dy, ld, n, n, m, o);
     }
     __syncthreads();
 }
 
+// Measurements of one sweep: each CTA adds its spin's part; the spin diagonals are
+// exchanged through distributed shared memory for the terms that need both spins, which
+// the spin-up CTA adds.  Entries both CTAs add to are accumulated atomically.
 template <typename T>
 __device__ void measure_t(const ChainDesc& d, TSmem<T>& sm) {
-    const int n = d.n;
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    const int n = d.n, sp = sm.spin;
     const size_t nn = (size_t)n * n;
-    const T* g0 = sm.g[0];
-    const T* g1 = sm.g[1];
+    const T* g = sm.g;
     double* obs = d.obs;
     for (int i = warp_id(); i < n; i += kNW)
         for (int j = lane_id(); j < n; j += 32) {
             const size_t e = (size_t)i * n + j;
-            d.gsum[e] += (double)g0[e];
-            d.gsum[nn + e] += (double)g1[e];
+            d.gsum[(size_t)sp * nn + e] += (double)g[e];
         }
-    double* nu = sm.xv[0];
-    double* nd = sm.xv[1];
+    double* nv = sm.xv[sp];
+    double* peer_nv = sm.peer_xv + (size_t)sp * n;
     for (int i = threadIdx.x; i < n; i += kNT) {
-        const double a = 1.0 - (double)g0[(size_t)i * n + i], b = 1.0 - (double)g1[(size_t)i * n + i];
-        nu[i] = a;
-        nd[i] = b;
-        obs[LQMC_OBS_HEADER + i] += a + b;
-        obs[LQMC_OBS_HEADER + n + i] += a * b;
+        const double a = 1.0 - (double)g[(size_t)i * n + i];
+        nv[i] = a;
+        peer_nv[i] = a;
     }
-    __syncthreads();
+    cluster.sync();
+    const double* nu = sm.xv[0];
+    const double* nd = sm.xv[1];
     double ek = 0.0, ep = 0.0, dc = 0.0, dn = 0.0;
     for (int j = warp_id(); j < n; j += kNW)
         for (int k = lane_id(); k < n; k += 32) {
             const double kv = d.kinetic[(size_t)j * n + k];
-            if (kv != 0.0) {
-                const double del = (j == k) ? 1.0 : 0.0;
-                ek += kv * ((del - (double)g0[(size_t)k * n + j]) + (del - (double)g1[(size_t)k * n + j]));
-            }
+            if (kv != 0.0) ek += kv * (((j == k) ? 1.0 : 0.0) - (double)g[(size_t)k * n + j]);
         }
-    for (int i = threadIdx.x; i < n; i += kNT) {
-        ep += (nu[i] - 0.5) * (nd[i] - 0.5);
-        dc += nu[i] * nd[i];
-        dn += nu[i] + nd[i];
+    if (sp == 0) {
+        for (int i = threadIdx.x; i < n; i += kNT) {
+            obs[LQMC_OBS_HEADER + i] += nu[i] + nd[i];
+            obs[LQMC_OBS_HEADER + n + i] += nu[i] * nd[i];
+            ep += (nu[i] - 0.5) * (nd[i] - 0.5);
+            dc += nu[i] * nd[i];
+            dn += nu[i] + nd[i];
+        }
     }
     ek = block_sum(ek, sm.sv);
     ep = block_sum(ep, sm.sv);
     dc = block_sum(dc, sm.sv);
     dn = block_sum(dn, sm.sv);
     if (threadIdx.x == 0) {
-        obs[0] += 1.0;
-        obs[1] += ek;
-        obs[2] += d.u * ep;
-        obs[3] += dc / n;
-        obs[4] += dn / n;
+        atomicAdd(&obs[1], ek);
+        if (sp == 0) {
+            obs[0] += 1.0;
+            obs[2] += d.u * ep;
+            obs[3] += dc / n;
+            obs[4] += dn / n;
+        }
     }
     double* onn = obs + LQMC_OBS_HEADER + 2 * n;
     double* osz = onn + nn;
+    const double* ns = sm.xv[sp];
     for (int i = warp_id(); i < n; i += kNW)
-      for (int j = lane_id(); j < n; j += 32) {
-        const size_t e = (size_t)i * n + j;
-        const double del = (i == j) ? 1.0 : 0.0;
-        const double same = nu[i] * nu[j] + nd[i] * nd[j] +
-                            (del - (double)g0[(size_t)j * n + i]) * (double)g0[e] +
-                            (del - (double)g1[(size_t)j * n + i]) * (double)g1[e];
-        const double cross = nu[i] * nd[j] + nd[i] * nu[j];
-        onn[e] += same + cross;
-        osz[e] += 0.25 * (same - cross);
-    }
+        for (int j = lane_id(); j < n; j += 32) {
+            const size_t e = (size_t)i * n + j;
+            const double del = (i == j) ? 1.0 : 0.0;
+            const double same = ns[i] * ns[j] + (del - (double)g[(size_t)j * n + i]) * (double)g[e];
+            const double cross = sp == 0 ? nu[i] * nd[j] + nd[i] * nu[j] : 0.0;
+            atomicAdd(&onn[e], same + cross);
+            atomicAdd(&osz[e], 0.25 * (same - cross));
+        }
     __syncthreads();
 }
 
 }  // namespace
 
 template <typename T, bool EMU>
-__global__ void __launch_bounds__(kNT, 1)
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kNT, 1)
 sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_measure) {
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
     extern __shared__ __align__(16) double smem[];
     __shared__ ChainDesc d;
     __shared__ int accepted;
     __shared__ int singular;
     __shared__ long long sub[3];
+    __shared__ double peer_resid;
+    const int sp = (int)cluster.block_rank();   // spin of this CTA
     if (threadIdx.x == 0) {
-        d = descs[blockIdx.x];
+        d = descs[blockIdx.x >> 1];
         accepted = 0;
         singular = 0;
         sub[0] = sub[1] = sub[2] = 0;
+        peer_resid = 0.0;
     }
     __syncthreads();
     const int n = d.n;
     const size_t nn = (size_t)n * n;
     TiledLayout<T> lay(n, d.n_chunks, EMU);
     unsigned char* w = reinterpret_cast<unsigned char*>(d.work);
+    unsigned char* wb = w + (size_t)sp * lay.spin_block;   // this spin's block
     TSmem<T> sm;
-    sm.g[0] = reinterpret_cast<T*>(w + lay.g);
-    sm.g[1] = sm.g[0] + nn;
-    sm.z0 = reinterpret_cast<T*>(w + lay.z);
+    sm.spin = sp;
+    sm.g = reinterpret_cast<T*>(wb + lay.g);
+    sm.z0 = reinterpret_cast<T*>(wb + lay.z);
     sm.z1 = sm.z0 + nn;
-    sm.s0 = reinterpret_cast<double*>(w + lay.s);
+    sm.s0 = reinterpret_cast<double*>(wb + lay.s);
     sm.s1 = sm.s0 + nn;
     sm.slots = w + lay.g_slots;
     sm.slot_bytes = lay.slot;
@@ -802,20 +813,18 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     constexpr size_t stage_region = (EMU && ozk::stage_bytes() > tile_gemm_smem<T>())
                                         ? ozk::stage_bytes() : tile_gemm_smem<T>();
     tp = sm.stage + stage_region / sizeof(T);
-    sm.oz.slices = reinterpret_cast<__nv_bfloat16*>(w + lay.oz);
-    sm.oz.ea = reinterpret_cast<int*>(w + lay.oz_ea);
+    sm.oz.slices = reinterpret_cast<__nv_bfloat16*>(wb + lay.oz);
+    sm.oz.ea = reinterpret_cast<int*>(wb + lay.oz_ea);
     sm.oz.eb = sm.oz.ea + n;
     const size_t dsz = (size_t)n * (d.delay + 1);
-    sm.dx[0] = tp; tp += dsz;
-    sm.dx[1] = tp; tp += dsz;
-    sm.dy[0] = tp; tp += dsz;
-    sm.dy[1] = tp; tp += dsz;
+    sm.dx = tp; tp += dsz;
+    sm.dy = tp; tp += dsz;
     {
         // LU panel over the delayed-update buffers (not in use during a refresh), then the
         // pivot list and the float64 staging buffer
-        double* lp = reinterpret_cast<double*>(sm.dx[0]);
+        double* lp = reinterpret_cast<double*>(sm.dx);
         sm.panel = lp;
-        const size_t dbytes = 4 * dsz * sizeof(T);
+        const size_t dbytes = 2 * dsz * sizeof(T);
         const size_t pbytes = (size_t)n * (panel_width(n) + 1) * sizeof(double);
         unsigned char* q = reinterpret_cast<unsigned char*>(lp) + (dbytes > pbytes ? dbytes : pbytes);
         q = reinterpret_cast<unsigned char*>(((uintptr_t)q + 15) & ~(uintptr_t)15);
@@ -823,9 +832,12 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
         q += kPanel * sizeof(int);
         sm.stage64 = reinterpret_cast<double*>(q);
     }
+    // the partner CTA's exchange buffers
+    sm.peer_gii = cluster.map_shared_rank(sm.gii, (unsigned)(sp ^ 1));
+    sm.peer_xv = cluster.map_shared_rank(sm.xv[0], (unsigned)(sp ^ 1));
+    cluster.sync();   // both CTAs set up before any remote write
 
-    double max_resid = 0.0;
-    double logdet[2] = {0.0, 0.0}, sgn[2] = {1.0, 1.0};
+    double max_resid = 0.0, logdet = 0.0, sgn = 1.0;
     uint64_t sweep_id = (uint64_t)d.diag[7];
     long long ph[5] = {0, 0, 0, 0, 0};   // clock cycles per phase (thread 0)
     long long tc = clock64();
@@ -837,10 +849,9 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
         tc = t_;                            \
     } while (0)
     for (int sw = 0; sw < n_sweeps; ++sw, ++sweep_id) {
-        right_stack_t<T, EMU>(d, sm, 0, &logdet[0], &sgn[0], &singular);
-        right_stack_t<T, EMU>(d, sm, 1, &logdet[1], &sgn[1], &singular);
+        right_stack_t<T, EMU>(d, sm, sp, &logdet, &sgn, &singular);
         LQMC_PHASE(0);
-        int lp[2] = {0, 0};
+        int lp = 0;
         for (int c = d.n_chunks - 1; c >= 0; --c) {
             const int lo = c * d.stab_every, hi = min(lo + d.stab_every, d.L);
             for (int l = hi - 1; l >= lo; --l) {
@@ -850,49 +861,45 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
                 LQMC_PHASE(2);
             }
             if (c > 0) {
-                for (int s = 0; s < 2; ++s) {
-                    left_step_t<T, EMU>(d, sm, s, lp[s], c == d.n_chunks - 1, lo, hi);
-                    lp[s] ^= 1;
-                    const int rs = s * d.n_chunks + c - 1, ls = 2 * d.n_chunks + 2 * s + lp[s];
-                    const double r = green_udt_t<T, EMU>(
-                        d, sm, slot_U(sm, rs, nn), slot_d(sm, rs, nn), slot_T(sm, rs, nn),
-                        slot_d(sm, rs, nn)[n], slot_U(sm, ls, nn), slot_d(sm, ls, nn),
-                        slot_T(sm, ls, nn), slot_d(sm, ls, nn)[n], sm.g[s], true, &logdet[s],
-                        &sgn[s], &singular);
-                    max_resid = fmax(max_resid, r);
-                }
+                left_step_t<T, EMU>(d, sm, sp, lp, c == d.n_chunks - 1, lo, hi);
+                lp ^= 1;
+                const int rs = sp * d.n_chunks + c - 1, ls = 2 * d.n_chunks + 2 * sp + lp;
+                const double r = green_udt_t<T, EMU>(
+                    d, sm, slot_U(sm, rs, nn), slot_d(sm, rs, nn), slot_T(sm, rs, nn),
+                    slot_d(sm, rs, nn)[n], slot_U(sm, ls, nn), slot_d(sm, ls, nn),
+                    slot_T(sm, ls, nn), slot_d(sm, ls, nn)[n], sm.g, true, &logdet, &sgn, &singular);
+                max_resid = fmax(max_resid, r);
                 LQMC_PHASE(3);
             }
         }
         __syncthreads();
         if (do_measure) measure_t<T>(d, sm);
         LQMC_PHASE(4);
-#undef LQMC_PHASE
         int bad = 0;
-        for (size_t e = threadIdx.x; e < 2 * nn; e += kNT) {
-            const double v = (e < nn) ? (double)sm.g[0][e] : (double)sm.g[1][e - nn];
-            if (!isfinite(v)) bad = 1;
-        }
+        for (size_t e = threadIdx.x; e < nn; e += kNT)
+            if (!isfinite((double)sm.g[e])) bad = 1;
         bad = __syncthreads_or(bad);
         if (bad && threadIdx.x == 0) atomicOr(d.status, LQMC_STATUS_NONFINITE);
     }
-    for (size_t e = threadIdx.x; e < nn; e += kNT) {
-        d.green[e] = (double)sm.g[0][e];
-        d.green[nn + e] = (double)sm.g[1][e];
-    }
+#undef LQMC_PHASE
+    for (size_t e = threadIdx.x; e < nn; e += kNT) d.green[(size_t)sp * nn + e] = (double)sm.g[e];
+    // the spin-down CTA hands its residual to the spin-up CTA, which writes the diagnostics
+    if (sp == 1 && threadIdx.x == 0) *cluster.map_shared_rank(&peer_resid, 0u) = max_resid;
+    cluster.sync();
     if (threadIdx.x == 0) {
-        d.diag[0] += (double)accepted;
-        d.diag[1] += (double)n_sweeps * n * d.L;
-        d.diag[2] = max_resid;
-        d.diag[3] = logdet[0];
-        d.diag[4] = logdet[1];
-        d.diag[5] = sgn[0];
-        d.diag[6] = sgn[1];
-        d.diag[7] += (double)n_sweeps;
-        for (int k = 0; k < 5; ++k) d.diag[8 + k] = (double)ph[k];
-        for (int k = 0; k < 3; ++k) d.diag[13 + k] = (double)sub[k];
+        d.diag[3 + sp] = logdet;
+        d.diag[5 + sp] = sgn;
         if (singular) atomicOr(d.status, LQMC_STATUS_SINGULAR);
-        if (max_resid > d.drift_tol) atomicOr(d.status, LQMC_STATUS_DRIFT);
+        if (sp == 0) {
+            max_resid = fmax(max_resid, peer_resid);
+            d.diag[0] += (double)accepted;
+            d.diag[1] += (double)n_sweeps * n * d.L;
+            d.diag[2] = max_resid;
+            d.diag[7] += (double)n_sweeps;
+            for (int k = 0; k < 5; ++k) d.diag[8 + k] = (double)ph[k];
+            for (int k = 0; k < 3; ++k) d.diag[13 + k] = (double)sub[k];
+            if (max_resid > d.drift_tol) atomicOr(d.status, LQMC_STATUS_DRIFT);
+        }
     }
 }
 
@@ -904,7 +911,7 @@ size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu) {
     const size_t tvec = 6 * (size_t)n * ts;                     // T vectors, bytes
     v += ((tvec + 7) / 8 + 3) & ~(size_t)3;
     v += 4;                                                     // gii
-    const size_t dbytes = 4 * (size_t)n * (delay + 1) * ts;
+    const size_t dbytes = 2 * (size_t)n * (delay + 1) * ts;
     const size_t pbytes = (size_t)n * (panel_width(n) + 1) * sizeof(double);
     size_t stage = fp32 ? tile_gemm_smem<float>() : tile_gemm_smem<double>();
     if (emu && ozk::stage_bytes() > stage) stage = ozk::stage_bytes();
@@ -931,7 +938,8 @@ static cudaError_t launch_tiled(const ChainDesc* d_descs, int n_chains, size_t s
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    sweep_tiled_kernel<T, EMU><<<n_chains, kNT, smem, stream>>>(d_descs, n_sweeps, measure);
+    // two CTAs (one cluster) per chain
+    sweep_tiled_kernel<T, EMU><<<2 * n_chains, kNT, smem, stream>>>(d_descs, n_sweeps, measure);
     return cudaGetLastError();
 }
 
