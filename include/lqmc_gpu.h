@@ -80,8 +80,10 @@ extern "C" {
  *   [8..12] SM clock cycles of the last lqmc_sweep spent per phase (thread 0 of the chain's
  *   CTA): [8] from-scratch recompute of G, [9] site updates, [10] wraps, [11] stabilisation
  *   refreshes, [12] measurements; tiled kernel only, cycles inside those phases spent in
- *   [13] Householder QR, [14] forming Q and T of the UDT factors, [15] LU solves.            */
-#define LQMC_DIAG_LEN 16
+ *   [13] Householder QR, [14] forming Q and T of the UDT factors, [15] LU solves,
+ *   [16] splitting operands of emulated float64 GEMMs, [17] their tensor-core loops.
+ *   [18..23] reserved.                                                                        */
+#define LQMC_DIAG_LEN 24
 
 typedef struct lqmc_params {
     int32_t mode;          /* LQMC_MODE_*                                                  */

@@ -21,7 +21,7 @@ RNGS = {"replay": 0, "philox": 1}
 ENGINES = {"auto": 0, "smem": 1, "tiled": 2}
 STATUS_NONFINITE, STATUS_SINGULAR, STATUS_DRIFT = 1, 2, 4
 OBS_HEADER = 8
-DIAG_LEN = 16
+DIAG_LEN = 24
 
 
 def obs_len(n):

@@ -5,7 +5,8 @@
 // thread, k staged through shared memory 16 at a time.  Every output is one fma chain in increasing k starting from zero, so the
 // result is independent of the tiling.  Inputs of another type (float / double) are
 // converted when they are staged.  Epilogue options: scale rows (rs) and columns (cs) of
-// the product, and subtract the product from C instead of overwriting it.
+// the product, and subtract the product from C instead of overwriting it.  The call begins
+// and ends with a block barrier, so operands written just before it are seen.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -46,6 +47,7 @@ __device__ void tile_gemm(T* __restrict__ c, int ldc, const TAIn* a, int lda, co
     T* bs = stage + kTileK * (D + 1);      // [kTileK][D + 1], bs[p][j] = B(p0 + p, j0 + j)
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     const int tiles_m = (m + D - 1) / D, tiles_n = (n + D - 1) / D;
+    __syncthreads();   // callers may have just written A or B without a barrier
     for (int tile = 0; tile < tiles_m * tiles_n; ++tile) {
         const int i0 = (tile / tiles_n) * D, j0 = (tile % tiles_n) * D;
         T acc[R][R];
@@ -54,21 +56,33 @@ __device__ void tile_gemm(T* __restrict__ c, int ldc, const TAIn* a, int lda, co
 #pragma unroll
             for (int s = 0; s < R; ++s) acc[r][s] = T(0);
         for (int p0 = 0; p0 < k; p0 += kTileK) {
-            __syncthreads();
-            for (int e = threadIdx.x; e < kTileK * D; e += kNT) {
+            // load the step's elements as one batch of independent loads, then store them
+            constexpr int kPerThread = kTileK * D / kNT;
+            static_assert(kTileK * D % kNT == 0, "staging must divide evenly over the block");
+            T va[kPerThread], vb[kPerThread];
+#pragma unroll
+            for (int r = 0; r < kPerThread; ++r) {
+                const int e = threadIdx.x + r * kNT;
                 // consecutive threads walk the contiguous index of each operand
                 int i, p;
                 if (TA) { p = e / D; i = e % D; } else { i = e / kTileK; p = e % kTileK; }
                 const int gi = i0 + i, gp = p0 + p;
-                T va = T(0);
-                if (gi < m && gp < k) va = (T)(TA ? a[(size_t)gp * lda + gi] : a[(size_t)gi * lda + gp]);
-                as[p * (D + 1) + i] = va;
+                va[r] = (gi < m && gp < k) ? (T)(TA ? a[(size_t)gp * lda + gi] : a[(size_t)gi * lda + gp]) : T(0);
                 int q, j;
                 if (TB) { j = e / kTileK; q = e % kTileK; } else { q = e / D; j = e % D; }
                 const int gq = p0 + q, gj = j0 + j;
-                T vb = T(0);
-                if (gq < k && gj < n) vb = (T)(TB ? b[(size_t)gj * ldb + gq] : b[(size_t)gq * ldb + gj]);
-                bs[q * (D + 1) + j] = vb;
+                vb[r] = (gq < k && gj < n) ? (T)(TB ? b[(size_t)gj * ldb + gq] : b[(size_t)gq * ldb + gj]) : T(0);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < kPerThread; ++r) {
+                const int e = threadIdx.x + r * kNT;
+                int i, p;
+                if (TA) { p = e / D; i = e % D; } else { i = e / kTileK; p = e % kTileK; }
+                as[p * (D + 1) + i] = va[r];
+                int q, j;
+                if (TB) { j = e / kTileK; q = e % kTileK; } else { q = e / D; j = e % D; }
+                bs[q * (D + 1) + j] = vb[r];
             }
             __syncthreads();
             const int pk = min(kTileK, k - p0);

@@ -151,6 +151,49 @@ __device__ void split_cols(const double* b, int ldb, int k, int n, __nv_bfloat16
     }
 }
 
+// words (2 bf16) of one k step staged per thread: A part then B part
+constexpr int kWordsA = kSlices * kTM * (kTK / 2) / kNT;   // 16
+constexpr int kWordsB = kSlices * kTN * (kTK / 2) / kNT;   // 8
+static_assert(kSlices * kTM * (kTK / 2) % kNT == 0 && kSlices * kTN * (kTK / 2) % kNT == 0,
+              "staging words must divide evenly over the block");
+
+__device__ __forceinline__ void load_step(const __nv_bfloat16* sa, const __nv_bfloat16* sb, int m,
+                                          int n, int kp, int i0, int j0, int p0,
+                                          uint32_t (&buf)[kWordsA + kWordsB]) {
+#pragma unroll
+    for (int r = 0; r < kWordsA; ++r) {
+        const int w = threadIdx.x + r * kNT;
+        const int t = w / (kTM * (kTK / 2)), row = (w / (kTK / 2)) % kTM, q = w % (kTK / 2);
+        buf[r] = (i0 + row < m)
+                     ? *reinterpret_cast<const uint32_t*>(sa + ((size_t)t * m + i0 + row) * kp + p0 + 2 * q)
+                     : 0u;
+    }
+#pragma unroll
+    for (int r = 0; r < kWordsB; ++r) {
+        const int w = threadIdx.x + r * kNT;
+        const int t = w / (kTN * (kTK / 2)), row = (w / (kTK / 2)) % kTN, q = w % (kTK / 2);
+        buf[kWordsA + r] = (j0 + row < n)
+                               ? *reinterpret_cast<const uint32_t*>(sb + ((size_t)t * n + j0 + row) * kp + p0 + 2 * q)
+                               : 0u;
+    }
+}
+
+__device__ __forceinline__ void store_step(__nv_bfloat16* as, __nv_bfloat16* bs,
+                                           const uint32_t (&buf)[kWordsA + kWordsB]) {
+#pragma unroll
+    for (int r = 0; r < kWordsA; ++r) {
+        const int w = threadIdx.x + r * kNT;
+        const int t = w / (kTM * (kTK / 2)), row = (w / (kTK / 2)) % kTM, q = w % (kTK / 2);
+        *reinterpret_cast<uint32_t*>(as + ((size_t)t * kTM + row) * kAPad + 2 * q) = buf[r];
+    }
+#pragma unroll
+    for (int r = 0; r < kWordsB; ++r) {
+        const int w = threadIdx.x + r * kNT;
+        const int t = w / (kTN * (kTK / 2)), row = (w / (kTK / 2)) % kTN, q = w % (kTK / 2);
+        *reinterpret_cast<uint32_t*>(bs + ((size_t)t * kTN + row) * kAPad + 2 * q) = buf[kWordsA + r];
+    }
+}
+
 __device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], uint32_t b0, uint32_t b1) {
     asm volatile(
         "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
@@ -164,6 +207,7 @@ struct Workspace {
     int* ea;                 // m
     int* eb;                 // n
     unsigned char* stage;    // stage_bytes() of shared memory
+    long long* cycles;       // optional [2] clock cycles: splitting, tensor-core loop (thread 0)
 };
 
 // C (m x n, ldc) = op(A) op(B) with float64 accuracy (see the header comment); epilogue as
@@ -174,9 +218,13 @@ __device__ void oz_gemm(double* c, int ldc, const double* a, int lda, const doub
     const int kp = kpad(k);
     __nv_bfloat16* sa = ws.slices;
     __nv_bfloat16* sb = ws.slices + (size_t)kSlices * m * kp;
+    __syncthreads();   // callers may have just written A or B without a barrier
+    const long long t0 = clock64();
     split_rows<TA>(a, lda, m, k, sa, ws.ea);
     split_cols<TB>(b, ldb, k, n, sb, ws.eb);
     __syncthreads();
+    const long long t1 = clock64();
+    if (ws.cycles && threadIdx.x == 0) ws.cycles[0] += t1 - t0;
     __nv_bfloat16* as = reinterpret_cast<__nv_bfloat16*>(ws.stage);       // [t][kTM][kAPad]
     __nv_bfloat16* bs = as + (size_t)kSlices * kTM * kAPad;                // [t][kTN][kAPad]
     const int lane = lane_id(), g = lane >> 2, tig = lane & 3;
@@ -199,24 +247,11 @@ __device__ void oz_gemm(double* c, int ldc, const double* a, int lda, const doub
                     for (int y = 0; y < 4; ++y) acc[d][x][y] = 0.f;
             const int c1 = min(kp, c0 + kChunk);
             for (int p0 = c0; p0 < c1; p0 += kTK) {
+                // the step's slice words: one batch of independent loads, then the stores
+                uint32_t buf[kWordsA + kWordsB];
+                load_step(sa, sb, m, n, kp, i0, j0, p0, buf);
                 __syncthreads();
-                // stage kTK columns of every slice: 32-bit words (2 bf16)
-                constexpr int wa = kSlices * kTM * (kTK / 2), wb = kSlices * kTN * (kTK / 2);
-                for (int w = threadIdx.x; w < wa + wb; w += kNT) {
-                    uint32_t val = 0;
-                    if (w < wa) {
-                        const int t = w / (kTM * (kTK / 2)), r = (w / (kTK / 2)) % kTM, q = w % (kTK / 2);
-                        if (i0 + r < m)
-                            val = *reinterpret_cast<const uint32_t*>(sa + ((size_t)t * m + i0 + r) * kp + p0 + 2 * q);
-                        *reinterpret_cast<uint32_t*>(as + ((size_t)t * kTM + r) * kAPad + 2 * q) = val;
-                    } else {
-                        const int w2 = w - wa;
-                        const int t = w2 / (kTN * (kTK / 2)), r = (w2 / (kTK / 2)) % kTN, q = w2 % (kTK / 2);
-                        if (j0 + r < n)
-                            val = *reinterpret_cast<const uint32_t*>(sb + ((size_t)t * n + j0 + r) * kp + p0 + 2 * q);
-                        *reinterpret_cast<uint32_t*>(bs + ((size_t)t * kTN + r) * kAPad + 2 * q) = val;
-                    }
-                }
+                store_step(as, bs, buf);
                 __syncthreads();
 #pragma unroll
                 for (int t = 0; t < kSlices; ++t) {
@@ -275,6 +310,7 @@ __device__ void oz_gemm(double* c, int ldc, const double* a, int lda, const doub
             }
     }
     __syncthreads();
+    if (ws.cycles && threadIdx.x == 0) ws.cycles[1] += clock64() - t1;
 }
 
 }  // namespace ozk

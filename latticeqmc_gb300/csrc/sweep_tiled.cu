@@ -84,9 +84,9 @@ struct TSmem {
     double* gii;  // [2 parity][2 spins] diagonal of G_eff for the current site, both spins
     long long* sub;   // [3] clock cycles: Householder QR, Q and T formation, LU solve
     ozk::Workspace oz;    // emulated float64 GEMM: slice buffers, exponents, staging
-    double* panel;    // blocked LU panel, n x (kPanel + 1); aliases dx/dy (not live then)
+    double* panel;    // blocked LU panel, n x (panel_width + 1); overlays stage, dx, dy
     int* piv;         // [kPanel] panel pivots
-    double* stage64;  // float64 GEMM staging of the LU
+    double* stage64;  // float64 GEMM staging of the LU (float kernel; same region as stage)
 };
 
 template <typename T> __device__ __forceinline__ T* slot_U(const TSmem<T>& sm, int idx, size_t nn) {
@@ -181,6 +181,15 @@ __device__ int householder_qr_cm(double* s, double* tau, int n, double* sv) {
 }
 
 // Solve W Z = R in place (both n x n, row-major, global memory) by a blocked right-looking
+// bytes of the GEMM staging region: the kernel's own GEMM (tiled T, or emulated), and in the
+// float kernel also the float64 tiled GEMM of the LU
+__host__ __device__ constexpr size_t stage_region_bytes(bool fp32, bool emu) {
+    size_t b = fp32 ? tile_gemm_smem<float>() : tile_gemm_smem<double>();
+    if (emu && ozk::stage_bytes() > b) b = ozk::stage_bytes();
+    if (fp32 && tile_gemm_smem<double>() > b) b = tile_gemm_smem<double>();
+    return b;
+}
+
 // LU with partial pivoting: each 32-column panel is factorised in shared memory (pivot =
 // first maximal |entry|, as LAPACK), its row interchanges applied across W and R, and the
 // trailing submatrix and R updated with tiled float64 GEMMs; then blocked back substitution.
@@ -760,14 +769,14 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     __shared__ ChainDesc d;
     __shared__ int accepted;
     __shared__ int singular;
-    __shared__ long long sub[3];
+    __shared__ long long sub[5];
     __shared__ double peer_resid;
     const int sp = (int)cluster.block_rank();   // spin of this CTA
     if (threadIdx.x == 0) {
         d = descs[blockIdx.x >> 1];
         accepted = 0;
         singular = 0;
-        sub[0] = sub[1] = sub[2] = 0;
+        sub[0] = sub[1] = sub[2] = sub[3] = sub[4] = 0;
         peer_resid = 0.0;
     }
     __syncthreads();
@@ -810,27 +819,26 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     sm.gii = p; p += 4;
     sm.stage = reinterpret_cast<T*>(p);
     sm.oz.stage = reinterpret_cast<unsigned char*>(p);
-    constexpr size_t stage_region = (EMU && ozk::stage_bytes() > tile_gemm_smem<T>())
-                                        ? ozk::stage_bytes() : tile_gemm_smem<T>();
+    sm.stage64 = p;   // the float64 LU staging (float kernel) shares the staging region
+    constexpr size_t stage_region = stage_region_bytes(sizeof(T) == 4, EMU);
     tp = sm.stage + stage_region / sizeof(T);
     sm.oz.slices = reinterpret_cast<__nv_bfloat16*>(wb + lay.oz);
     sm.oz.ea = reinterpret_cast<int*>(wb + lay.oz_ea);
     sm.oz.eb = sm.oz.ea + n;
+    sm.oz.cycles = sub + 3;
     const size_t dsz = (size_t)n * (d.delay + 1);
     sm.dx = tp; tp += dsz;
     sm.dy = tp; tp += dsz;
     {
-        // LU panel over the delayed-update buffers (not in use during a refresh), then the
-        // pivot list and the float64 staging buffer
-        double* lp = reinterpret_cast<double*>(sm.dx);
-        sm.panel = lp;
-        const size_t dbytes = 2 * dsz * sizeof(T);
+        // The LU panel overlays the GEMM staging and the delayed-update buffers: the panel is
+        // live only between a panel load and the trailing-update GEMMs, and X / Y only
+        // between refreshes.  The pivot list follows the larger of the two.
+        sm.panel = p;
+        const size_t rbytes = stage_region + 2 * dsz * sizeof(T);
         const size_t pbytes = (size_t)n * (panel_width(n) + 1) * sizeof(double);
-        unsigned char* q = reinterpret_cast<unsigned char*>(lp) + (dbytes > pbytes ? dbytes : pbytes);
+        unsigned char* q = reinterpret_cast<unsigned char*>(p) + (rbytes > pbytes ? rbytes : pbytes);
         q = reinterpret_cast<unsigned char*>(((uintptr_t)q + 15) & ~(uintptr_t)15);
         sm.piv = reinterpret_cast<int*>(q);
-        q += kPanel * sizeof(int);
-        sm.stage64 = reinterpret_cast<double*>(q);
     }
     // the partner CTA's exchange buffers
     sm.peer_gii = cluster.map_shared_rank(sm.gii, (unsigned)(sp ^ 1));
@@ -897,7 +905,7 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
             d.diag[2] = max_resid;
             d.diag[7] += (double)n_sweeps;
             for (int k = 0; k < 5; ++k) d.diag[8 + k] = (double)ph[k];
-            for (int k = 0; k < 3; ++k) d.diag[13 + k] = (double)sub[k];
+            for (int k = 0; k < 5; ++k) d.diag[13 + k] = (double)sub[k];
             if (max_resid > d.drift_tol) atomicOr(d.status, LQMC_STATUS_DRIFT);
         }
     }
@@ -911,12 +919,9 @@ size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu) {
     const size_t tvec = 6 * (size_t)n * ts;                     // T vectors, bytes
     v += ((tvec + 7) / 8 + 3) & ~(size_t)3;
     v += 4;                                                     // gii
-    const size_t dbytes = 2 * (size_t)n * (delay + 1) * ts;
+    const size_t rbytes = stage_region_bytes(fp32, emu) + 2 * (size_t)n * (delay + 1) * ts;
     const size_t pbytes = (size_t)n * (panel_width(n) + 1) * sizeof(double);
-    size_t stage = fp32 ? tile_gemm_smem<float>() : tile_gemm_smem<double>();
-    if (emu && ozk::stage_bytes() > stage) stage = ozk::stage_bytes();
-    return v * sizeof(double) + stage + (dbytes > pbytes ? dbytes : pbytes) + 16 +
-           kPanel * sizeof(int) + tile_gemm_smem<double>();
+    return v * sizeof(double) + (rbytes > pbytes ? rbytes : pbytes) + 16 + kPanel * sizeof(int);
 }
 
 // largest delayed-update depth <= requested (0: 32 in fp32, 16 in fp64) that fits `cap`

@@ -210,7 +210,8 @@ class Engine:
                 "logdet": d[3:5].copy(), "sign": d[5:7].copy(), "sweeps": int(d[7]),
                 "phase_cycles": {"recompute": d[8], "update": d[9], "wrap": d[10],
                                  "stabilise": d[11], "measure": d[12]},
-                "sub_cycles": {"qr": d[13], "q_and_t": d[14], "lu": d[15]}}
+                "sub_cycles": {"qr": d[13], "q_and_t": d[14], "lu": d[15],
+                               "oz_split": d[16], "oz_mma": d[17]}}
 
     def status(self):
         s = np.empty(len(self.chains), dtype=np.int32)

@@ -48,7 +48,8 @@ def main():
     tot = max(sum(pc.values()), 1.0)
     print(f"{a.side}x{a.side} L={a.L} {a.precision} chains={a.chains}: "
           f"{dt * 1e3 / a.sweeps:.1f} ms/sweep, residual {d['max_residual']:.1e}, "
-          + " ".join(f"{k}={100 * v / tot:.1f}%" for k, v in pc.items()))
+          + " ".join(f"{k}={100 * v / tot:.1f}%" for k, v in pc.items()) + " | "
+          + " ".join(f"{k}={100 * v / tot:.1f}%" for k, v in d["sub_cycles"].items()))
     eng.close()
 
 
