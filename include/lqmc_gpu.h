@@ -50,8 +50,9 @@ extern "C" {
 #define LQMC_PREC_FP64 0     /* every floating-point operation in float64                */
 #define LQMC_PREC_MIXED 1    /* float32 G, wraps and delayed updates; FP64 stabilisation */
 #define LQMC_PREC_FP64E 2    /* float64 G and updates; every dense product a float64-accurate
-                                GEMM emulated on the BF16 tensor cores (49-bit sliced operands,
-                                exact FP32 accumulation); FP64 Householder QR                 */
+                                GEMM emulated on the tcgen05 BF16 tensor cores (48-bit sliced
+                                operands, exact FP32 accumulation in tensor memory); FP64
+                                Householder QR                                               */
 
 /* uniform-draw sources */
 #define LQMC_RNG_REPLAY 0    /* caller uploads the uniforms (e.g. numpy's stream)        */
@@ -61,6 +62,8 @@ extern "C" {
 #define LQMC_STATUS_NONFINITE 1   /* NaN/Inf found in G                                  */
 #define LQMC_STATUS_SINGULAR 2    /* zero pivot in an LU factorisation                   */
 #define LQMC_STATUS_DRIFT 4       /* stabilisation residual above the drift threshold    */
+#define LQMC_STATUS_TIMEOUT 8     /* a bounded device-side wait (tensor-core pipeline) ran
+                                     out; the chain's results since then are not valid     */
 
 /* observable vector layout returned by lqmc_get_observables (per chain), float64:
  *   [0] number of measurements       [1] sum of kinetic energy   [2] sum of potential energy
@@ -81,8 +84,9 @@ extern "C" {
  *   CTA): [8] from-scratch recompute of G, [9] site updates, [10] wraps, [11] stabilisation
  *   refreshes, [12] measurements; tiled kernel only, cycles inside those phases spent in
  *   [13] Householder QR, [14] forming Q and T of the UDT factors, [15] LU solves,
- *   [16] splitting operands of emulated float64 GEMMs, [17] their tensor-core loops.
- *   [18..23] reserved.                                                                        */
+ *   [16] splitting operands of emulated float64 GEMMs, [17] their tensor-core loops
+ *   (including [18]), [18] their epilogues (reading and combining the accumulators).
+ *   [19..23] reserved.                                                                        */
 #define LQMC_DIAG_LEN 24
 
 typedef struct lqmc_params {
@@ -95,8 +99,14 @@ typedef struct lqmc_params {
     uint64_t seed;         /* Philox key word 0 (LQMC_RNG_PHILOX)                          */
     int32_t device;        /* CUDA device ordinal                                          */
     int32_t engine;        /* LQMC_ENGINE_*: which sweep kernel runs the chains            */
-    int32_t reserved[6];
+    int32_t debug;         /* LQMC_DEBUG_* bits; 0 in production                           */
+    int32_t reserved[5];
 } lqmc_params;
+
+/* debug bits (lqmc_params.debug), for testing the failure paths */
+#define LQMC_DEBUG_STALL_TC_WAIT 1  /* emulated-GEMM kernel: the first tensor-core step issues
+                                       no copies, so its bounded wait runs out (about a second)
+                                       and the chain reports LQMC_STATUS_TIMEOUT              */
 
 /* sweep kernels (lqmc_params.engine) */
 #define LQMC_ENGINE_AUTO 0   /* shared-memory kernel for fp64 and n <= 128, else tiled        */

@@ -19,7 +19,8 @@ MODES = {"compat": 0, "dqmc": 1}
 PRECISIONS = {"fp64": 0, "mixed": 1, "fp64e": 2}
 RNGS = {"replay": 0, "philox": 1}
 ENGINES = {"auto": 0, "smem": 1, "tiled": 2}
-STATUS_NONFINITE, STATUS_SINGULAR, STATUS_DRIFT = 1, 2, 4
+STATUS_NONFINITE, STATUS_SINGULAR, STATUS_DRIFT, STATUS_TIMEOUT = 1, 2, 4, 8
+DEBUG_STALL_TC_WAIT = 1
 OBS_HEADER = 8
 DIAG_LEN = 24
 
@@ -32,7 +33,7 @@ class Params(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("precision", ctypes.c_int32), ("rng", ctypes.c_int32),
                 ("stab_every", ctypes.c_int32), ("delay", ctypes.c_int32), ("record", ctypes.c_int32),
                 ("seed", ctypes.c_uint64), ("device", ctypes.c_int32), ("engine", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 6)]
+                ("debug", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
 
 
 class LqmcError(RuntimeError):
@@ -97,11 +98,12 @@ class Handle:
     """Owns one lqmc_handle; every call checks the return code."""
 
     def __init__(self, mode, precision, rng, stab_every, delay, seed, record, device,
-                 engine="auto"):
+                 engine="auto", debug=0):
         self.lib = load()
         p = Params(mode=MODES[mode], precision=PRECISIONS[precision], rng=RNGS[rng],
                    stab_every=int(stab_every), delay=int(delay), record=int(bool(record)),
-                   seed=int(seed) & ((1 << 64) - 1), device=int(device), engine=ENGINES[engine])
+                   seed=int(seed) & ((1 << 64) - 1), device=int(device), engine=ENGINES[engine],
+                   debug=int(debug))
         h = ctypes.c_void_p()
         rc = self.lib.lqmc_create(ctypes.byref(p), ctypes.byref(h))
         if rc != LQMC_OK:

@@ -16,8 +16,8 @@ namespace lqmc {
 size_t sweep_fp64_smem_bytes(int n, int flags);
 cudaError_t launch_sweep_fp64(const ChainDesc* d_descs, int n_chains, size_t smem, int n_sweeps,
                               int measure, cudaStream_t stream);
-size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu);
-int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap, bool emu);
+size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu, int stages);
+int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap, bool emu, int stages);
 size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32, bool emu);
 cudaError_t launch_sweep_tiled(const ChainDesc* d_descs, int n_chains, size_t smem, int precision,
                                int n_sweeps, int measure, cudaStream_t stream);
@@ -243,6 +243,7 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
         for (int k = 0; k < 4; ++k) d.c[k] = exp_consts[4 * c + k];
         d.u = u[c];
         d.drift_tol = 1e-6;
+        d.debug = h->p.debug;
         if (h->p.precision == LQMC_PREC_MIXED) kind[c] = kTiledFp32;
         else if (h->p.precision == LQMC_PREC_FP64E) kind[c] = kTiledFp64e;
         else if (h->p.engine == LQMC_ENGINE_TILED) kind[c] = kTiledFp64;
@@ -264,8 +265,11 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
         } else {
             const bool f32 = kind[c] == kTiledFp32, emu = kind[c] == kTiledFp64e;
             d.flags = 0;
-            d.delay = lqmc::sweep_tiled_delay(n, f32, h->p.delay, smem_cap, emu);
-            smem[c] = lqmc::sweep_tiled_smem_bytes(n, f32, d.delay, emu);
+            // two tensor-core stage buffers unless they would cost delayed-update depth
+            d.oz_stages = 1;
+            d.delay = lqmc::sweep_tiled_delay(n, f32, h->p.delay, smem_cap, emu, 1);
+            if (emu && lqmc::sweep_tiled_delay(n, f32, h->p.delay, smem_cap, emu, 2) >= d.delay) d.oz_stages = 2;
+            smem[c] = lqmc::sweep_tiled_smem_bytes(n, f32, d.delay, emu, d.oz_stages);
             work = (lqmc::sweep_tiled_work_bytes(n, d.n_chunks, f32, emu) + 7) / 8;
             if (smem[c] > smem_cap) { release(h); return fail(h, LQMC_ERR_UNSUPPORTED, "lattice too large for shared memory"); }
         }

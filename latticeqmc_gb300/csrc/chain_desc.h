@@ -42,6 +42,8 @@ struct ChainDesc {
     const float* expk_f;      // float copies of expk / expkinv (mixed-precision engine)
     const float* expkinv_f;
     int32_t delay;            // tiled kernel: rank-k depth of the delayed updates (>= 1)
+    int32_t oz_stages;        // tiled kernel, emulated GEMMs: tensor-core stage buffers (1 or 2)
+    int32_t debug;            // LQMC_DEBUG_* bits
     int32_t pad1;
 };
 

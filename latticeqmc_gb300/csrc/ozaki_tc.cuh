@@ -1,0 +1,496 @@
+// Float64-accurate GEMM on the 5th-generation (tcgen05) tensor cores for one CTA of
+// blk::kNT threads (Ozaki-style operand splitting, exact integer slice products).
+//
+// Row i of op(A) is scaled by 2^-E_i (E_i = exponent just above its largest entry) and
+// written as a 48-bit fixed-point integer F = trunc(|a| 2^(48 - E_i)) cut into kSlices = 8
+// six-bit slices q_t in [-63, 63] (exact in bfloat16); columns of op(B) likewise with 2^-F_j.
+// Then C_ij = 2^(E_i + F_j - 54) sum_{d<8} 2^(6 (7 - d)) D_d with D_d = sum_{t+u=d} (A_t B_u)_ij,
+// keeping the 36 leading slice pairs.  Each A_t B_u is a tcgen05.mma (kind::f16, BF16 x BF16
+// -> FP32, M = 128, K = 16) accumulating into the TMEM columns of diagonal d, so the eight
+// accumulators of a 128 x 64 output tile fill the 512 TMEM columns.  The FP32 sums are exact
+// integers while |D_d| <= 8 k 63^2 < 2^24, i.e. for k <= kMaxK = 512; longer products are
+// cut into chunks of kMaxK whose results are added in float64.  The only roundings are the
+// truncation of the operands at 2^-48 of their row / column maximum and the final
+// conversion to float64.  A row (column) holding a NaN or Inf gives NaN in its output row
+// (column).
+//
+// Data movement: the split writes every slice directly in the tensor core's canonical
+// K-major, no-swizzle layout (8 x 16-byte core matrices), grouped so that all eight slices
+// of one (row block, 16-wide k step) are one contiguous block.  One thread then moves a
+// whole k step of A (32 KB) and of B (16 KB) into shared memory with two bulk asynchronous
+// copies completing on an mbarrier, issues the 36 MMAs of the step and commits them to a
+// second mbarrier; with two stage buffers the copies of step s + 1 overlap the MMAs of step
+// s.  The epilogue reads the accumulators with tcgen05.ld (warp w reads TMEM lanes
+// 32 (w mod 4) ..), combines them in int64 and scales by exponent arithmetic.
+//
+// Every wait is bounded: a wait that runs out sets Tc::fail, after which this and every later
+// call return without issuing work; the kernel reports the flag as a status bit.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "block_fp64.cuh"
+#include "block_gemm.cuh"
+
+namespace lqmc {
+namespace ozt {
+
+using namespace blk;
+
+constexpr int kSlices = 8;
+constexpr int kBits = 6;
+constexpr int kWidth = kSlices * kBits;
+constexpr int kBM = 128, kBN = 64, kBK = 16;
+constexpr int kTileA = kBM * kBK;             // bf16 elements of one slice tile of A (4 KB)
+constexpr int kTileB = kBN * kBK;             // one slice tile of B (2 KB)
+constexpr int kStepA = kSlices * kTileA;      // all slices of one (row block, k step)
+constexpr int kStepB = kSlices * kTileB;
+constexpr int kMaxK = 512;                    // exact FP32 diagonal sums up to this k
+constexpr int kTmemCols = kSlices * kBN;      // 512: the whole tensor memory of the SM
+constexpr int kNonFinite = 1 << 20;
+constexpr long long kWaitCycles = 2000000000ll;   // ~1 s of SM clock before a wait gives up
+
+// shared-memory bytes of `stages` stage buffers (1 or 2)
+__host__ __device__ constexpr size_t stage_bytes(int stages) {
+    return (size_t)stages * (kStepA + kStepB) * sizeof(__nv_bfloat16);
+}
+
+__host__ __device__ constexpr int kpad(int k) { return (k + kBK - 1) / kBK * kBK; }
+__host__ __device__ constexpr int rows_pad(int m, int blk) { return (m + blk - 1) / blk * blk; }
+
+// bf16 elements of the slice buffers of an (m x k) times (k x n) product
+__host__ __device__ constexpr size_t slice_elems(int m, int n, int k) {
+    return (size_t)kSlices * ((size_t)rows_pad(m, kBM) + rows_pad(n, kBN)) * kpad(k);
+}
+
+// element offset of (row r, k index q) inside one slice tile: core matrix (r / 8, q / 8) at
+// (r / 8) * 128 + (q / 8) * 64 elements (SBO = 256 B, LBO = 128 B), 8 x 8 elements inside
+__device__ __forceinline__ int core_offset(int r, int q) {
+    return (r >> 3) * 128 + (q >> 3) * 64 + (r & 7) * 8 + (q & 7);
+}
+
+// per-CTA state of the tensor-core path (static shared memory of the kernel)
+struct Tc {
+    unsigned long long bar[4];   // copies done [2], MMAs done [2]
+    uint32_t tmem;               // TMEM base address (lane 0, first column)
+    uint32_t phase;              // parity bits of the four barriers (thread 0)
+    int fail;                    // a wait ran out
+    int stall;                   // test hook: the next step issues no copies (its wait runs out)
+};
+
+struct Workspace {
+    __nv_bfloat16* slices;   // slice_elems(m, n, k) bf16, 16-byte aligned
+    int* ea;                 // m
+    int* eb;                 // n
+    unsigned char* stage;    // stage_bytes(stages) of shared memory, 128-byte aligned
+    int stages;              // 1 or 2
+    Tc* tc;
+    long long* cycles;       // optional [3]: splitting, whole product loop, its epilogues (thread 0)
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// ---- TMEM and barrier set-up, once per kernel --------------------------------------------
+
+// warp 0 allocates the 512 TMEM columns; all threads initialise after a barrier
+__device__ inline void tc_setup(Tc* tc) {
+    if (warp_id() == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n"
+                     :: "r"(smem_u32(&tc->tmem)), "r"(kTmemCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 4; ++i)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&tc->bar[i])));
+        tc->phase = 0;
+        tc->fail = 0;
+        tc->stall = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+}
+
+// warp 0 frees the TMEM columns; every MMA has completed (each call waits for its last commit)
+__device__ inline void tc_teardown(Tc* tc) {
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (warp_id() == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n"
+                     :: "r"(tc->tmem), "r"(kTmemCols));
+}
+
+// bounded parity wait; false when about kWaitCycles passed without the phase completing
+__device__ __forceinline__ bool bar_wait(unsigned long long* bar, uint32_t parity) {
+    const uint32_t a = smem_u32(bar);
+    const long long t0 = clock64();
+    for (;;) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done) : "r"(a), "r"(parity) : "memory");
+        if (done) return true;
+        if (clock64() - t0 > kWaitCycles) return false;
+    }
+}
+
+// ---- splitting ---------------------------------------------------------------------------
+
+// 48-bit fixed-point magnitude of v for exponent e (|v| < 2^e), 0 for zero / non-finite
+__device__ __forceinline__ unsigned long long fixed48(double v, int e) {
+    const long long bits = __double_as_longlong(v);
+    const int be = (int)((bits >> 52) & 0x7FF);
+    if (be == 0 || be == 0x7FF || e == kNonFinite) return 0;
+    const unsigned long long mant = ((unsigned long long)bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = (be - 1075) + kWidth - e;
+    if (sh >= 0) return (sh < 11) ? (mant << sh) : 0;
+    return (-sh < 64) ? (mant >> (-sh)) : 0;
+}
+
+// Split X (rows x k), X(r, q) = trans ? x[q ld + r] : x[r ld + q], into the tile layout with
+// row blocks of BLK rows: slice t of (row block rb, k step s) at
+// ((rb * S + s) * kSlices + t) * BLK * kBK, S = kpad(k) / kBK.  Rows >= `rows` and k >= `k`
+// are zero.  exps[r] = E_r.  `scratch` is shared memory of at least rows ints.
+//
+// Both passes read 8 consecutive elements of memory per unit with independent loads, so
+// many L2 requests are in flight: the row maxima of the biased exponents are gathered with
+// shared-memory atomics (an exponent of 0x7FF, NaN or Inf, dominates and marks the row).
+template <int BLK>
+__device__ void split_tiles(const double* x, int ld, bool trans, int rows, int k, int* exps,
+                            __nv_bfloat16* dst, int* scratch) {
+    const int kp = kpad(k), S = kp / kBK, rp = rows_pad(rows, BLK);
+    for (int r = threadIdx.x; r < rows; r += kNT) scratch[r] = 0;
+    __syncthreads();
+    if (!trans) {
+        // unit (r, q8): x[r ld + 8 q8 ..]
+        const int g8 = (k + 7) / 8;
+        for (int u = threadIdx.x; u < rows * g8; u += kNT) {
+            const int r = u / g8, q0 = (u % g8) * 8;
+            int emax = 0;
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                if (q0 + c < k)
+                    emax = max(emax, (int)((__double_as_longlong(x[(size_t)r * ld + q0 + c]) >> 52) & 0x7FF));
+            atomicMax(&scratch[r], emax);
+        }
+    } else {
+        // unit (q, r8): x[q ld + 8 r8 ..], eight rows
+        const int g8 = (rows + 7) / 8;
+        for (int u = threadIdx.x; u < k * g8; u += kNT) {
+            const int q = u / g8, r0 = (u % g8) * 8;
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                if (r0 + c < rows)
+                    atomicMax(&scratch[r0 + c],
+                              (int)((__double_as_longlong(x[(size_t)q * ld + r0 + c]) >> 52) & 0x7FF));
+        }
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < rows; r += kNT) {
+        const int emax = scratch[r];
+        exps[r] = (emax == 0x7FF) ? kNonFinite : (emax == 0 ? 0 : emax - 1022);
+    }
+    __syncthreads();
+    // slices: one unit = one row and 8 consecutive k; consecutive threads take consecutive
+    // rows, so each slice's 16-byte stores are contiguous within a core matrix
+    const int groups = kp / 8;
+#pragma unroll 2
+    for (int u = threadIdx.x; u < rp * groups; u += kNT) {
+        const int r = u % rp, g = u / rp, q0 = g * 8;
+        const int e = (r < rows) ? exps[r] : 0;
+        // 48-bit magnitudes as two 24-bit halves (slices 0-3 and 4-7), sign masks per pair
+        uint32_t fh[8], fl[8], sgn[4];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+            const int q = q0 + c;
+            double v = 0.0;
+            if (r < rows && q < k) v = trans ? x[(size_t)q * ld + r] : x[(size_t)r * ld + q];
+            const unsigned long long f = fixed48(v, e);
+            fh[c] = (uint32_t)(f >> 24);
+            fl[c] = (uint32_t)f & 0xFFFFFFu;
+            if (c & 1) sgn[c >> 1] |= (__double_as_longlong(v) < 0) ? 0x80000000u : 0u;
+            else sgn[c >> 1] = (__double_as_longlong(v) < 0) ? 0x8000u : 0u;
+        }
+        const int rb = r / BLK, rr = r % BLK, s = q0 / kBK;
+        __nv_bfloat16* base = dst + ((size_t)(rb * S + s) * kSlices) * (BLK * kBK) + core_offset(rr, q0 % kBK);
+#pragma unroll
+        for (int t = 0; t < kSlices; ++t) {
+            const int sh = kBits * (kSlices / 2 - 1 - (t & 3));
+            uint32_t w[4];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const uint32_t a0 = ((t < 4 ? fh[2 * c] : fl[2 * c]) >> sh) & 63u;
+                const uint32_t a1 = ((t < 4 ? fh[2 * c + 1] : fl[2 * c + 1]) >> sh) & 63u;
+                // small integers are exact in float (2^23 magic) and in bfloat16
+                const float f0 = __uint_as_float(0x4B000000u | a0) - 8388608.0f;
+                const float f1 = __uint_as_float(0x4B000000u | a1) - 8388608.0f;
+                const __nv_bfloat162 p = __floats2bfloat162_rn(f0, f1);
+                w[c] = *reinterpret_cast<const uint32_t*>(&p) | sgn[c];
+            }
+            *reinterpret_cast<uint4*>(base + (size_t)t * (BLK * kBK)) = make_uint4(w[0], w[1], w[2], w[3]);
+        }
+    }
+}
+
+// ---- tensor-core issue -------------------------------------------------------------------
+
+// shared-memory matrix descriptor: K-major, no swizzle, LBO = 128 B (next core matrix in k),
+// SBO = 256 B (next 8 rows), descriptor version 1
+__device__ __forceinline__ unsigned long long smem_desc(uint32_t addr) {
+    return (unsigned long long)((addr & 0x3FFFF) >> 4) | ((unsigned long long)(128 >> 4) << 16) |
+           ((unsigned long long)(256 >> 4) << 32) | (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: D F32, A and B BF16, both K-major, M = 128, N = nn
+// (a multiple of 16 up to 256)
+__host__ __device__ constexpr uint32_t idesc(int nn) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(nn >> 3) << 17) | ((uint32_t)(kBM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t d_tmem, unsigned long long a, unsigned long long b,
+                                    uint32_t id, uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+        :: "r"(d_tmem), "l"(a), "l"(b), "r"(id), "r"(accumulate));
+}
+
+__device__ __forceinline__ void commit(unsigned long long* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n"
+                 :: "r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes,
+                                          unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
+                 :: "r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void expect_tx(unsigned long long* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n"
+                 :: "r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// 8 consecutive TMEM columns of this thread's lane (no wait)
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7])
+        : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait() {
+    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
+// The epilogue stays off the float64 pipe (a few operations per clock per SM on this part)
+// and keeps its integer work short and branch-free.
+
+// t * 2^s as float64, rounded to nearest-even, t != 0, |t| < 2^63
+__device__ __forceinline__ double scaled_double(long long t, int s) {
+    const unsigned long long sign = (unsigned long long)t & (1ull << 63);
+    const unsigned long long a = t < 0 ? (unsigned long long)(-t) : (unsigned long long)t;
+    const int nb = 64 - __clzll((long long)a);              // bit length, 1 .. 63
+    const int sh = nb - 53;                                  // > 0: bits to round away
+    const int shr = sh > 0 ? sh : 0, shl = sh > 0 ? 0 : -sh;
+    unsigned long long mant = (a >> shr) << shl;
+    const unsigned long long rem = a & ((1ull << shr) - 1ull);
+    const unsigned long long half = sh > 0 ? (1ull << (shr - 1)) : 1ull;
+    mant += (rem > half || (rem == half && (mant & 1ull))) ? 1ull : 0ull;
+    const int be = nb - 1 + 1023 + s;
+    if (be > 0 && be < 0x7FF - 1)
+        // a rounding carry to 2^53 moves into the exponent field
+        return __longlong_as_double((long long)(sign | (((unsigned long long)be << 52) + (mant - (1ull << 52)))));
+    // subnormal or overflowing result: assemble at unit scale and let ldexp round
+    const double unit = __longlong_as_double((long long)(sign | (((unsigned long long)(nb - 1 + 1023) << 52) +
+                                                                  (mant - (1ull << 52)))));
+    return ldexp(unit, s);
+}
+
+// ---- the product -------------------------------------------------------------------------
+
+// C (m x n, ldc) = op(A) op(B) with float64 accuracy; epilogue as blk::tile_gemm (row /
+// column scale, subtract).  A(i, p) = TA ? a[p lda + i] : a[i lda + p];
+// B(p, j) = TB ? b[j ldb + p] : b[p ldb + j].
+template <bool TA, bool TB>
+__device__ void oz_gemm_tc(double* c, int ldc, const double* a, int lda, const double* b, int ldb,
+                           int m, int n, int k, const Workspace& ws, GemmOpt<double> opt = GemmOpt<double>()) {
+    Tc* tc = ws.tc;
+    // callers may have just written A or B; order earlier generic shared-memory use of the
+    // stage before the asynchronous copies into it
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    __syncthreads();
+    if (tc->fail || m <= 0 || n <= 0) return;
+    if (k <= 0) {
+        // empty sum: C = 0, or C unchanged when subtracting
+        if (!opt.subtract)
+            for (int e = threadIdx.x; e < m * n; e += kNT) c[(size_t)(e / n) * ldc + e % n] = 0.0;
+        __syncthreads();
+        return;
+    }
+    const int kp = kpad(k), S = kp / kBK;
+    __nv_bfloat16* sa = ws.slices;
+    __nv_bfloat16* sb = ws.slices + (size_t)kSlices * rows_pad(m, kBM) * kp;
+    const long long t0 = clock64();
+    int* scratch = reinterpret_cast<int*>(ws.stage);   // the stage is idle while splitting
+    split_tiles<kBM>(a, lda, TA, m, k, ws.ea, sa, scratch);
+    split_tiles<kBN>(b, ldb, !TB, n, k, ws.eb, sb, scratch);
+    // the slices were written through the generic proxy and are read by bulk copies
+    asm volatile("fence.proxy.async;\n" ::: "memory");
+    __syncthreads();
+    const long long t1 = clock64();
+    if (ws.cycles && threadIdx.x == 0) ws.cycles[0] += t1 - t0;
+
+    const int stages = ws.stages;
+    const uint32_t tmem = tc->tmem;
+    const int tiles_m = rows_pad(m, kBM) / kBM, tiles_n = rows_pad(n, kBN) / kBN;
+    const int chunk_steps = kMaxK / kBK;
+    const int w = warp_id(), lane = lane_id();
+    const int row = 32 * (w & 3) + lane;          // TMEM lane = output row of the tile
+    bool failed = false;
+    for (int tile = 0; tile < tiles_m * tiles_n; ++tile) {
+        const int tm = tile / tiles_n, tn = tile % tiles_n;
+        const int i0 = tm * kBM, j0 = tn * kBN;
+        for (int s0 = 0; s0 < S; s0 += chunk_steps) {
+            const int steps = min(chunk_steps, S - s0);
+            if (threadIdx.x == 0 && !failed) {
+                uint32_t ph = tc->phase;
+                auto load = [&](int s, int buf) {
+                    unsigned char* st = ws.stage + (size_t)buf * (kStepA + kStepB) * 2;
+                    expect_tx(&tc->bar[buf], (kStepA + kStepB) * 2);
+                    bulk_load(st, sa + (size_t)(tm * S + s0 + s) * kStepA, kStepA * 2, &tc->bar[buf]);
+                    bulk_load(st + kStepA * 2, sb + (size_t)(tn * S + s0 + s) * kStepB, kStepB * 2, &tc->bar[buf]);
+                };
+                auto wait = [&](int i) -> bool {
+                    const bool ok = bar_wait(&tc->bar[i], (ph >> i) & 1u);
+                    ph ^= 1u << i;
+                    return ok;
+                };
+                if (tc->stall) tc->stall = 0;   // test hook: nothing will complete the first wait
+                else for (int s = 0; s < min(stages, steps); ++s) load(s, s);
+                for (int s = 0; s < steps && !failed; ++s) {
+                    const int buf = s % stages;
+                    if (!wait(buf)) { failed = true; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                    const uint32_t st = smem_u32(ws.stage + (size_t)buf * (kStepA + kStepB) * 2);
+                    // A_t times the stacked B_0 .. B_{7-t}: the accumulators of diagonals
+                    // t .. 7 are the contiguous TMEM columns [64 t, 512), so one MMA of
+                    // N = 64 (8 - t) (cut at 256) covers every pair of this t
+#pragma unroll
+                    for (int t = 0; t < kSlices; ++t) {
+                        constexpr int kMaxN = 256;
+#pragma unroll
+                        for (int off = 0; off < (kSlices - t) * kBN; off += kMaxN) {
+                            const int nn = min(kMaxN, (kSlices - t) * kBN - off);
+                            mma(tmem + (uint32_t)(t * kBN + off), smem_desc(st + t * kTileA * 2),
+                                smem_desc(st + kStepA * 2 + (off / kBN) * kTileB * 2), idesc(nn),
+                                (s > 0 || t > 0) ? 1u : 0u);
+                        }
+                    }
+                    commit(&tc->bar[2 + buf]);
+                    if (stages == 2) {
+                        if (s >= 1) {
+                            if (!wait(2 + (s - 1) % 2)) { failed = true; break; }
+                            if (s + 1 < steps) load(s + 1, (s + 1) % 2);
+                        }
+                    } else {
+                        if (!wait(2)) { failed = true; break; }
+                        if (s + 1 < steps) load(s + 1, 0);
+                    }
+                }
+                if (!failed && stages == 2 && !wait(2 + (steps - 1) % 2)) failed = true;
+                tc->phase = ph;
+                if (failed) tc->fail = 1;
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            if (tc->fail) return;
+            const long long te = clock64();
+            // epilogue, in two halves of 32 columns: each thread combines 16 outputs of its
+            // row (two groups of 8 columns, all 8 diagonals read before one wait), the half is
+            // transposed through the stage buffer, and written with whole-row coalesced stores
+            double* ts = reinterpret_cast<double*>(ws.stage);   // [kBM][kTs]
+            constexpr int kTs = 33;
+            const int ei = (i0 + row < m) ? ws.ea[i0 + row] : 0;
+#pragma unroll 1
+            for (int h = 0; h < 2; ++h) {
+#pragma unroll 1
+                for (int g = 0; g < 2; ++g) {
+                    const int cl = 16 * (w >> 2) + 8 * g;   // column within the half
+                    const int ct = 32 * h + cl;             // column within the tile
+                    int ej[8];
+#pragma unroll
+                    for (int x = 0; x < 8; ++x) ej[x] = (j0 + ct + x < n) ? ws.eb[j0 + ct + x] : 0;
+                    uint32_t r[kSlices][8];
+#pragma unroll
+                    for (int d = 0; d < kSlices; ++d)
+                        tmem_ld8(tmem + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)(d * kBN + ct), r[d]);
+                    tmem_wait();
+#pragma unroll
+                    for (int x = 0; x < 8; ++x) {
+                        // T = sum_d D_d 2^(6 (7 - d)) / 16 by Horner: |D_d| < 2^24 is exact in
+                        // int32 (D_0 64 + D_1 < 2^31), |T| < 2^63; dropping the low 4 bits of D_7
+                        // is far below the 2^-48 truncation of the operands
+                        int q[kSlices];
+#pragma unroll
+                        for (int d = 0; d < kSlices; ++d) q[d] = __float2int_rn(__uint_as_float(r[d][x]));
+                        long long t = (long long)(q[0] * 64 + q[1]);
+#pragma unroll
+                        for (int d = 2; d < kSlices - 1; ++d) t = t * 64 + q[d];
+                        t = t * 4 + (q[kSlices - 1] >> 4);
+                        // C = T 2^(E_i + F_j - 2W + 6 (S - 1) + 4)
+                        double v = 0.0;
+                        if (t != 0) v = scaled_double(t, ei + ej[x] - 2 * kWidth + kBits * (kSlices - 1) + 4);
+                        if (ei == kNonFinite || ej[x] == kNonFinite) v = __longlong_as_double(0x7FF8000000000000ll);
+                        ts[row * kTs + cl + x] = v;
+                    }
+                }
+                __syncthreads();
+                // each warp writes 16 rows; their old values and scales are loaded first
+                const int gj = j0 + 32 * h + lane;
+                constexpr int kRowsW = kBM / kNW;
+                const bool read_c = opt.subtract || s0 > 0;
+                const double csj = (opt.cs && gj < n) ? opt.cs[gj] : 1.0;
+                double old_c[kRowsW], rsv[kRowsW];
+#pragma unroll
+                for (int q = 0; q < kRowsW; ++q) {
+                    const int gi = i0 + w + q * kNW;
+                    const bool ok = gi < m && gj < n;
+                    old_c[q] = (ok && read_c) ? c[(size_t)gi * ldc + gj] : 0.0;
+                    rsv[q] = (ok && opt.rs) ? opt.rs[gi] : 1.0;
+                }
+#pragma unroll
+                for (int q = 0; q < kRowsW; ++q) {
+                    const int rr = w + q * kNW, gi = i0 + rr;
+                    if (gi >= m || gj >= n) continue;
+                    double v = ts[rr * kTs + lane];
+                    if (opt.rs) v = rsv[q] * v;
+                    if (opt.cs) v = v * csj;
+                    c[(size_t)gi * ldc + gj] = opt.subtract ? old_c[q] - v : (s0 == 0 ? v : old_c[q] + v);
+                }
+                // generic accesses to the stage are ordered before later bulk copies into it
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                __syncthreads();
+            }
+            // every warp has read the accumulators before the next MMAs overwrite them
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            if (ws.cycles && threadIdx.x == 0) ws.cycles[2] += clock64() - te;
+        }
+    }
+    if (ws.cycles && threadIdx.x == 0) ws.cycles[1] += clock64() - t1;
+}
+
+}  // namespace ozt
+}  // namespace lqmc

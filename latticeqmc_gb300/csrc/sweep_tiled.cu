@@ -1,7 +1,7 @@
 // Persistent dqmc sweep kernel for large lattices and for mixed precision: a cluster of two
 // CTAs per Markov chain, one per spin, every n x n matrix in global memory (L2-resident for
 // tens of chains at N = 256), dense products through the block-tiled GEMM of
-// block_gemm.cuh or the emulated float64 GEMM of ozaki_gemm.cuh.  The spins only meet in
+// block_gemm.cuh or the emulated float64 GEMM of ozaki_tc.cuh.  The spins only meet in
 // the acceptance ratio R = R_up R_dn of each site, whose two factors the CTAs exchange
 // through distributed shared memory under one cluster barrier per site, and in the
 // measurements.
@@ -23,7 +23,7 @@
 #include "block_gemm.cuh"
 #include "chain_desc.h"
 #include "lqmc_gpu.h"
-#include "ozaki_gemm.cuh"
+#include "ozaki_tc.cuh"
 #include "philox.cuh"
 
 namespace lqmc {
@@ -45,7 +45,8 @@ struct TiledLayout {
         z = g + align256(nn * sizeof(T));                   // Z0, Z1 GEMM temps   (T)
         s = z + align256(2 * nn * sizeof(T));               // S0, S1 QR / LU      (double)
         oz = s + align256(2 * nn * sizeof(double));         // emulated GEMM slices (bf16)
-        const size_t oz_bytes = emu ? align256(ozk::slice_elems(n, n, n) * 2) : 0;
+        // the largest product of the kernel has m, n, k <= n_sites
+        const size_t oz_bytes = emu ? align256(ozt::slice_elems(n, n, n) * 2) : 0;
         oz_ea = oz + oz_bytes;                              // emulated GEMM exponents (int)
         spin_block = oz_ea + (emu ? align256(2 * (size_t)n * sizeof(int)) : 0);
         g_slots = 2 * spin_block;
@@ -83,7 +84,7 @@ struct TSmem {
     T* dy;        // Y (n x (kd + 1))
     double* gii;  // [2 parity][2 spins] diagonal of G_eff for the current site, both spins
     long long* sub;   // [3] clock cycles: Householder QR, Q and T formation, LU solve
-    ozk::Workspace oz;    // emulated float64 GEMM: slice buffers, exponents, staging
+    ozt::Workspace oz;    // emulated float64 GEMM: slice buffers, exponents, staging, TMEM state
     double* panel;    // blocked LU panel, n x (panel_width + 1); overlays stage, dx, dy
     int* piv;         // [kPanel] panel pivots
     double* stage64;  // float64 GEMM staging of the LU (float kernel; same region as stage)
@@ -100,13 +101,13 @@ template <typename T> __device__ __forceinline__ double* slot_d(const TSmem<T>& 
 }
 
 // Dense product of the tiled kernel: the block-tiled SIMT GEMM, or with EMU the float64
-// GEMM emulated on the BF16 tensor cores (ozaki_gemm.cuh).
+// GEMM emulated on the tcgen05 BF16 tensor cores (ozaki_tc.cuh).
 template <typename T, bool EMU, bool TA, bool TB, typename TAIn, typename TBIn>
 __device__ __forceinline__ void gemm_t(TSmem<T>& sm, T* c, int ldc, const TAIn* a, int lda,
                                        const TBIn* b, int ldb, int m, int n, int k,
                                        GemmOpt<T> o = GemmOpt<T>()) {
     if constexpr (EMU) {
-        ozk::oz_gemm<TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.oz, o);
+        ozt::oz_gemm_tc<TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.oz, o);
     } else {
         tile_gemm<T, TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.stage, o);
     }
@@ -181,14 +182,19 @@ __device__ int householder_qr_cm(double* s, double* tau, int n, double* sv) {
 }
 
 // Solve W Z = R in place (both n x n, row-major, global memory) by a blocked right-looking
-// bytes of the GEMM staging region: the kernel's own GEMM (tiled T, or emulated), and in the
-// float kernel also the float64 tiled GEMM of the LU
-__host__ __device__ constexpr size_t stage_region_bytes(bool fp32, bool emu) {
+// bytes of the GEMM staging region: the kernel's own GEMM (tiled T, or emulated with
+// `stages` tensor-core stage buffers), and in the float kernel also the float64 tiled GEMM of
+// the LU
+__host__ __device__ constexpr size_t stage_region_bytes(bool fp32, bool emu, int stages) {
     size_t b = fp32 ? tile_gemm_smem<float>() : tile_gemm_smem<double>();
-    if (emu && ozk::stage_bytes() > b) b = ozk::stage_bytes();
+    if (emu && ozt::stage_bytes(stages) > b) b = ozt::stage_bytes(stages);
     if (fp32 && tile_gemm_smem<double>() > b) b = tile_gemm_smem<double>();
     return b;
 }
+
+// An emulated-GEMM CTA owns all 512 TMEM columns of its SM: its shared memory is kept above
+// half of the SM's so that no second CTA can be resident there.
+constexpr size_t kEmuMinSmem = 120 * 1024;
 
 // LU with partial pivoting: each 32-column panel is factorised in shared memory (pivot =
 // first maximal |entry|, as LAPACK), its row interchanges applied across W and R, and the
@@ -769,17 +775,22 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     __shared__ ChainDesc d;
     __shared__ int accepted;
     __shared__ int singular;
-    __shared__ long long sub[5];
+    __shared__ long long sub[6];
+    __shared__ ozt::Tc tcs;
     __shared__ double peer_resid;
     const int sp = (int)cluster.block_rank();   // spin of this CTA
     if (threadIdx.x == 0) {
         d = descs[blockIdx.x >> 1];
         accepted = 0;
         singular = 0;
-        sub[0] = sub[1] = sub[2] = sub[3] = sub[4] = 0;
+        for (int k = 0; k < 6; ++k) sub[k] = 0;
         peer_resid = 0.0;
     }
     __syncthreads();
+    if constexpr (EMU) {
+        ozt::tc_setup(&tcs);   // TMEM columns and the pipeline's mbarriers
+        if (threadIdx.x == 0 && (d.debug & LQMC_DEBUG_STALL_TC_WAIT) && d.diag[7] == 0.0) tcs.stall = 1;
+    }
     const int n = d.n;
     const size_t nn = (size_t)n * n;
     TiledLayout<T> lay(n, d.n_chunks, EMU);
@@ -817,15 +828,18 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     p = reinterpret_cast<double*>(tp);
     p = smem + (((p - smem) + 3) & ~(ptrdiff_t)3);
     sm.gii = p; p += 4;
+    if (EMU) p = smem + (((p - smem) + 15) & ~(ptrdiff_t)15);   // 128-byte aligned stage
     sm.stage = reinterpret_cast<T*>(p);
     sm.oz.stage = reinterpret_cast<unsigned char*>(p);
+    sm.oz.stages = d.oz_stages;
+    sm.oz.tc = &tcs;
     sm.stage64 = p;   // the float64 LU staging (float kernel) shares the staging region
-    constexpr size_t stage_region = stage_region_bytes(sizeof(T) == 4, EMU);
+    const size_t stage_region = stage_region_bytes(sizeof(T) == 4, EMU, d.oz_stages);
     tp = sm.stage + stage_region / sizeof(T);
     sm.oz.slices = reinterpret_cast<__nv_bfloat16*>(wb + lay.oz);
     sm.oz.ea = reinterpret_cast<int*>(wb + lay.oz_ea);
     sm.oz.eb = sm.oz.ea + n;
-    sm.oz.cycles = sub + 3;
+    sm.oz.cycles = sub + 3;   // splitting, product loops, epilogues
     const size_t dsz = (size_t)n * (d.delay + 1);
     sm.dx = tp; tp += dsz;
     sm.dy = tp; tp += dsz;
@@ -905,29 +919,38 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
             d.diag[2] = max_resid;
             d.diag[7] += (double)n_sweeps;
             for (int k = 0; k < 5; ++k) d.diag[8 + k] = (double)ph[k];
-            for (int k = 0; k < 5; ++k) d.diag[13 + k] = (double)sub[k];
+            for (int k = 0; k < 6; ++k) d.diag[13 + k] = (double)sub[k];
             if (max_resid > d.drift_tol) atomicOr(d.status, LQMC_STATUS_DRIFT);
         }
+    }
+    if constexpr (EMU) {
+        if (threadIdx.x == 0 && tcs.fail) atomicOr(d.status, LQMC_STATUS_TIMEOUT);
+        ozt::tc_teardown(&tcs);
     }
 }
 
 // bytes of dynamic shared memory / per-chain global work of the tiled kernel
-size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu) {
+size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu, int stages) {
     size_t v = (size_t)(kNW + 8 + 9 * n);
     v = (v + 3) & ~(size_t)3;                                   // doubles
     const size_t ts = fp32 ? 4 : 8;
     const size_t tvec = 6 * (size_t)n * ts;                     // T vectors, bytes
     v += ((tvec + 7) / 8 + 3) & ~(size_t)3;
     v += 4;                                                     // gii
-    const size_t rbytes = stage_region_bytes(fp32, emu) + 2 * (size_t)n * (delay + 1) * ts;
+    const size_t rbytes = stage_region_bytes(fp32, emu, stages) + 2 * (size_t)n * (delay + 1) * ts;
     const size_t pbytes = (size_t)n * (panel_width(n) + 1) * sizeof(double);
-    return v * sizeof(double) + (rbytes > pbytes ? rbytes : pbytes) + 16 + kPanel * sizeof(int);
+    size_t total = v * sizeof(double) + (rbytes > pbytes ? rbytes : pbytes) + 16 + kPanel * sizeof(int);
+    if (emu) {
+        total += 128;   // stage alignment
+        if (total < kEmuMinSmem) total = kEmuMinSmem;
+    }
+    return total;
 }
 
 // largest delayed-update depth <= requested (0: 32 in fp32, 16 in fp64) that fits `cap`
-int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap, bool emu) {
+int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap, bool emu, int stages) {
     int k = requested > 0 ? requested : (fp32 ? 32 : 16);
-    while (k > 1 && sweep_tiled_smem_bytes(n, fp32, k, emu) > cap) --k;
+    while (k > 1 && sweep_tiled_smem_bytes(n, fp32, k, emu, stages) > cap) --k;
     return k;
 }
 

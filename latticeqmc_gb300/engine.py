@@ -83,7 +83,7 @@ class Engine:
     """
 
     def __init__(self, chains, mode="dqmc", precision="fp64", rng="philox", stab_every=None,
-                 delay=0, seed=0, record=False, device=0, engine="auto"):
+                 delay=0, seed=0, record=False, device=0, engine="auto", debug=0):
         self.chains = list(chains)
         if stab_every is None:
             stab_every = auto_stab_every(self.chains)
@@ -91,7 +91,7 @@ class Engine:
         self.mode, self.precision, self.rng = mode, precision, rng
         self.record = bool(record)
         self._h = _native.Handle(mode, precision, rng, stab_every, delay, seed, record, device,
-                                 engine)
+                                 engine, debug)
         n = len(self.chains)
         n_sites = np.array([c.n for c in self.chains], dtype=np.int32)
         n_slices = np.array([c.L for c in self.chains], dtype=np.int32)
@@ -211,7 +211,7 @@ class Engine:
                 "phase_cycles": {"recompute": d[8], "update": d[9], "wrap": d[10],
                                  "stabilise": d[11], "measure": d[12]},
                 "sub_cycles": {"qr": d[13], "q_and_t": d[14], "lu": d[15],
-                               "oz_split": d[16], "oz_mma": d[17]}}
+                               "oz_split": d[16], "oz_mma": d[17], "oz_epilogue": d[18]}}
 
     def status(self):
         s = np.empty(len(self.chains), dtype=np.int32)

@@ -150,3 +150,44 @@ def test_fp64e_against_fp64_engine_16x16_beta8():
     assert not (b.status() & 3).any()
     a.close()
     b.close()
+
+
+def test_fp64e_batched_chains_match_single_chain_runs():
+    """Chains of several sizes in one launch (one bucket per size, one CTA pair per chain)
+    give bit-identical G to the same chains run alone."""
+    specs, us = [], []
+    for side, seed in ((4, 1), (6, 2), (10, 3), (6, 4)):
+        K, field, rng = _setup(side, 2.0, 20, 900 + seed)
+        specs.append(ChainSpec(K, 4.0, 2.0, 20, field))
+        us.append(rng.random(side * side * 20))
+    both = Engine(specs, mode="dqmc", precision="fp64e", rng="replay", stab_every=5)
+    both.set_uniforms_all(np.concatenate(us))
+    both.sweep(1)
+    for c, (spec, u) in enumerate(zip(specs, us)):
+        one = Engine([spec], mode="dqmc", precision="fp64e", rng="replay", stab_every=5)
+        one.set_uniforms(0, u)
+        one.sweep(1)
+        assert np.array_equal(one.green(0), both.green(c))
+        one.close()
+    assert not both.status().any()
+    both.close()
+
+
+def test_fp64e_stalled_tensor_core_wait_reports_timeout():
+    """The tensor-core pipeline's waits are bounded: with the test hook that issues no
+    copies for the first step, the wait runs out (about a second), the chain reports
+    LQMC_STATUS_TIMEOUT, and the context stays usable for the next handle."""
+    from latticeqmc_gb300 import _native
+    K, field, rng = _setup(8, 2.0, 20, 77)
+    spec = ChainSpec(K, 4.0, 2.0, 20, field)
+    bad = Engine([spec], mode="dqmc", precision="fp64e", rng="philox", seed=3, stab_every=5,
+                 debug=_native.DEBUG_STALL_TC_WAIT)
+    bad.sweep(1)
+    st = bad.status()
+    assert st[0] & _native.STATUS_TIMEOUT
+    bad.close()
+    good = Engine([spec], mode="dqmc", precision="fp64e", rng="philox", seed=3, stab_every=5)
+    good.sweep(2)
+    assert not good.status().any()
+    assert np.isfinite(good.green(0)).all()
+    good.close()
