@@ -132,15 +132,21 @@ __device__ __forceinline__ void load_ev_t(const ChainDesc& d, TSmem<T>& sm, int 
     }
 }
 
-// Householder QR in place of a column-major matrix (element (i, j) at s[j n + i], so that
-// every column is contiguous in global memory); same convention as blk::householder_qr.
-__device__ int householder_qr_cm(double* s, double* tau, int n, double* sv) {
+// Householder QR of one panel of a column-major matrix (element (i, j) at s[j n + i], so
+// that every column is contiguous in global memory): columns jb .. jb+b-1, rows jb .. n-1,
+// each reflector applied only to the later columns of the panel (the trailing columns are
+// updated by the caller in compact WY form).  Same convention as blk::householder_qr:
+// beta = -sign(alpha) |x|, tau = (beta - alpha) / beta, v = x / (alpha - beta) with v_0 = 1
+// implicit, R's diagonal entry beta stored in place.  Returns the number of reflectors with
+// tau != 0.
+__device__ int householder_panel_cm(double* s, double* tau, int n, int jb, int b, double* sv) {
     const int lane = lane_id();
     int nrefl = 0;
-    for (int j = 0; j < n - 1; ++j) {
+    for (int j = jb; j < jb + b; ++j) {
         double* cj = s + (size_t)j * n;
         if (warp_id() == 0) {
             double ss = 0.0;
+#pragma unroll 4
             for (int i = j + 1 + lane; i < n; i += 32) { const double v = cj[i]; ss = fma(v, v, ss); }
             ss = warp_sum(ss);
             if (lane == 0) {
@@ -163,9 +169,10 @@ __device__ int householder_qr_cm(double* s, double* tau, int n, double* sv) {
         const double den = sv[kNW];
         for (int i = j + 1 + threadIdx.x; i < n; i += kNT) cj[i] = cj[i] / den;
         __syncthreads();
-        for (int k = j + 1 + warp_id(); k < n; k += kNW) {
+        for (int k = j + 1 + warp_id(); k < jb + b; k += kNW) {
             double* ck = s + (size_t)k * n;
             double acc = 0.0;
+#pragma unroll 4
             for (int i = j + 1 + lane; i < n; i += 32) acc = fma(cj[i], ck[i], acc);
             acc = warp_sum(acc);
             const double wk = t * (ck[j] + acc);
@@ -180,6 +187,44 @@ __device__ int householder_qr_cm(double* s, double* tau, int n, double* sv) {
     }
     return nrefl;
 }
+
+// Explicit V of the panel at jb (rows jb .. n-1, b columns; unit diagonal, zeros above),
+// column-major with leading dimension n - jb: v[c (n - jb) + i] = V(i, c).
+__device__ void panel_v(double* v, const double* s, int n, int jb, int b) {
+    const int rows = n - jb;
+    for (int e = threadIdx.x; e < rows * b; e += kNT) {
+        const int c = e / rows, i = e % rows;
+        v[e] = (i < c) ? 0.0 : (i == c ? 1.0 : s[(size_t)(jb + c) * n + jb + i]);
+    }
+    __syncthreads();
+}
+
+// T factor of the compact WY form H_jb ... H_{jb+b-1} = I - V T V^T (LAPACK dlarft, forward,
+// columnwise): T(i, i) = tau_i, T(0:i, i) = -tau_i T(0:i, 0:i) (V^T V)(0:i, i).  gram is V^T V
+// and tf the b x b row-major T (b <= 32: one lane per row).
+__device__ void wy_t_factor(double* tf, const double* gram, const double* tau, int b) {
+    if (warp_id() == 0) {
+        const int r = lane_id();
+        for (int i = 0; i < b; ++i) {
+            if (r < b) {
+                double v = 0.0;
+                if (r < i) {
+                    for (int q = r; q < i; ++q) v = fma(tf[r * b + q], gram[q * b + i], v);
+                    v *= -tau[i];
+                } else if (r == i) {
+                    v = tau[i];
+                }
+                tf[r * b + i] = v;
+            }
+            __syncwarp();
+        }
+    }
+    __syncthreads();
+}
+
+// panel width of the blocked QR; with bw <= n / 5 the scratch of udt_absorb_t
+// (ceil((n - 1) / bw) bw^2 + 3 n bw doubles) fits in the n^2 of S1
+__device__ __forceinline__ int qr_block(int n) { return min(32, max(1, n / 5)); }
 
 // Solve W Z = R in place (both n x n, row-major, global memory) by a blocked right-looking
 // bytes of the GEMM staging region: the kernel's own GEMM (tiled T, or emulated with
@@ -350,55 +395,43 @@ __device__ void lu_solve_dispatch<float, false>(TSmem<float>& sm, int n, double*
     lu_solve_blocked<false>(d, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
 }
 
-// Q = H_0 ... H_{n-2} in precision T, column-major (qc[k n + i] = Q[i][k]), from the
-// float64 column-major reflectors in s / tau.
-template <typename T>
-__device__ void form_q_cm_t(T* qc, const double* s, const double* tau, int n) {
-    const int lane = lane_id();
-    for (int k = warp_id(); k < n; k += kNW)
-        for (int i = lane; i < n; i += 32) qc[(size_t)k * n + i] = (i == k) ? T(1) : T(0);
-    __syncthreads();
-    for (int j = n - 2; j >= 0; --j) {
-        const T t = (T)tau[j];
-        if (t == T(0)) continue;
-        const double* vj = s + (size_t)j * n;
-        for (int k = j + warp_id(); k < n; k += kNW) {
-            T* qk = qc + (size_t)k * n;
-            T acc = T(0);
-            for (int i = j + 1 + lane; i < n; i += 32) acc = fma((T)vj[i], qk[i], acc);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            const T wk = t * (qk[j] + acc);
-            for (int i = j + lane; i < n; i += 32) {
-                const T vi = (i == j) ? T(1) : (T)vj[i];
-                qk[i] = fma(-vi, wk, qk[i]);
-            }
-        }
-        __syncthreads();
-    }
+// Float64 GEMM of the QR: the emulated tensor-core GEMM, or the float64 tiled GEMM on the
+// (shared) staging buffer.
+template <typename T, bool EMU, bool TA, bool TB>
+__device__ __forceinline__ void gemm64(TSmem<T>& sm, double* c, int ldc, const double* a, int lda,
+                                       const double* b, int ldb, int m, int n, int k,
+                                       GemmOpt<double> o = GemmOpt<double>()) {
+    if constexpr (EMU) ozt::oz_gemm_tc<TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.oz, o);
+    else tile_gemm<double, TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.stage64, o);
 }
 
 // UDT of Z diag(d_old) T_old (pre-pivoted QR, QR in float64).  z row-major; U is written
 // column-major (uc[k n + i] = U[i][k]), T row-major.  Returns det sign of U.
-template <typename T>
+//
+// Blocked Householder QR: each panel of qr_block(n) columns is factorised column by column,
+// then the trailing columns are updated in compact WY form C -= (V T^T)(V^T C) with GEMMs.
+// Q = Q_0 Q_1 ... is accumulated backwards with GEMMs (Q_p = I - V_p T_p V_p^T), and
+// T_new = diag(1 / d) R P^T T_old is one GEMM.  Scratch: S1 (the panels' T factors, V, V T
+// and the V^T C products) and Z0 (P^T T_old); z is dead once copied.
+template <typename T, bool EMU>
 __device__ double udt_absorb_t(const ChainDesc& d, TSmem<T>& sm, const T* z, const double* d_old,
                                const T* t_old, T* u_new, double* d_new, T* t_new) {
     const int n = d.n, lane = lane_id();
     // column norms of Z diag(d_old): lanes over columns (contiguous rows of z)
-    for (int k = threadIdx.x; k < n; k += kNT) sm.nrm[k] = 0.0;
-    __syncthreads();
     for (int k = threadIdx.x; k < n; k += kNT) {
         double acc = 0.0;
+#pragma unroll 8
         for (int i = 0; i < n; ++i) { const double v = (double)z[(size_t)i * n + k]; acc = fma(v, v, acc); }
         const double dk = d_old ? fabs(d_old[k]) : 1.0;
         sm.nrm[k] = sqrt(acc) * dk;
     }
     __syncthreads();
+    // descending order of the norms (ties by index, NaN last), compared as integer keys
     for (int k = threadIdx.x; k < n; k += kNT) {
-        const double v = isnan(sm.nrm[k]) ? -1.0 : sm.nrm[k];
+        const long long v = isnan(sm.nrm[k]) ? -1ll : __double_as_longlong(sm.nrm[k]);
         int rank = 0;
         for (int j = 0; j < n; ++j) {
-            const double w = isnan(sm.nrm[j]) ? -1.0 : sm.nrm[j];
+            const long long w = isnan(sm.nrm[j]) ? -1ll : __double_as_longlong(sm.nrm[j]);
             rank += (w > v) || (w == v && j < k);
         }
         sm.order[rank] = k;
@@ -411,31 +444,68 @@ __device__ double udt_absorb_t(const ChainDesc& d, TSmem<T>& sm, const T* z, con
             s[(size_t)r * n + i] = (double)z[(size_t)i * n + src] * (d_old ? d_old[src] : 1.0);
         }
     __syncthreads();
-    long long t0 = clock64();
-    const int nrefl = householder_qr_cm(s, sm.tau, n, sm.sv);
-    long long t1 = clock64();
+    const long long t0 = clock64();
+    const int bw = qr_block(n);
+    double* tstore = sm.s1;                       // panels' T factors, bw x bw each
+    double* vbuf = tstore + (size_t)((n - 2) / bw + 1) * bw * bw;   // V of a panel, column-major
+    double* ubuf = vbuf + (size_t)n * bw;         // V T^T (QR) or V T (Q), row-major
+    double* ybuf = ubuf + (size_t)n * bw;         // V^T V, V^T C, V^T Q
+    int nrefl = 0, npan = 0;
+    for (int jb = 0; jb < n - 1; jb += bw, ++npan) {
+        const int b = min(bw, n - 1 - jb), rows = n - jb, nc = n - jb - b;
+        nrefl += householder_panel_cm(s, sm.tau, n, jb, b, sm.sv);
+        panel_v(vbuf, s, n, jb, b);
+        double* tf = tstore + (size_t)npan * bw * bw;
+        gemm64<T, EMU, false, true>(sm, ybuf, b, vbuf, rows, vbuf, rows, b, b, rows);   // V^T V
+        wy_t_factor(tf, ybuf, sm.tau + jb, b);
+        if (nc > 0) {
+            // U = V T^T;  Y = V^T C;  C -= U Y  (as C^T -= Y^T U^T on the column-major s)
+            gemm64<T, EMU, true, true>(sm, ubuf, b, vbuf, rows, tf, b, rows, b, b);
+            double* ct = s + (size_t)(jb + b) * n + jb;
+            gemm64<T, EMU, false, true>(sm, ybuf, nc, vbuf, rows, ct, n, b, nc, rows);
+            GemmOpt<double> o;
+            o.subtract = true;
+            gemm64<T, EMU, true, true>(sm, ct, n, ybuf, nc, ubuf, b, nc, rows, b, o);
+        }
+    }
+    const long long t1 = clock64();
     if (threadIdx.x == 0) sm.sub[0] += t1 - t0;
     for (int i = threadIdx.x; i < n; i += kNT) {
         const double di = s[(size_t)i * n + i];
         sm.dv[i] = di;
         d_new[i] = di;
+        sm.xt[0][i] = (T)(1.0 / di);
+    }
+    // Q, backwards: Q[jb:, jb:] -= (V T)(V^T Q[jb:, jb:])
+    for (int k = warp_id(); k < n; k += kNW)
+        for (int i = lane; i < n; i += 32) u_new[(size_t)k * n + i] = (i == k) ? T(1) : T(0);
+    __syncthreads();
+    T* yq = reinterpret_cast<T*>(ybuf);
+    for (int p = npan - 1; p >= 0; --p) {
+        const int jb = p * bw, b = min(bw, n - 1 - jb), rows = n - jb;
+        panel_v(vbuf, s, n, jb, b);
+        gemm64<T, EMU, true, false>(sm, ubuf, b, vbuf, rows, tstore + (size_t)p * bw * bw, b, rows, b, b);
+        T* q2 = u_new + (size_t)jb * n + jb;
+        gemm_t<T, EMU, false, true>(sm, yq, rows, vbuf, rows, q2, n, b, rows, rows);
+        GemmOpt<T> o;
+        o.subtract = true;
+        gemm_t<T, EMU, true, true>(sm, q2, n, yq, rows, (const double*)ubuf, b, rows, rows, b, o);
+    }
+    // T_new = diag(1 / d) R (P^T T_old): R's strict lower part (the reflectors) cleared, the
+    // rows of T_old gathered in the pivot order
+    for (int k = warp_id(); k < n; k += kNW)
+        for (int i = k + 1 + lane; i < n; i += 32) s[(size_t)k * n + i] = 0.0;
+    T* tg = sm.z0;
+    for (int k = warp_id(); k < n; k += kNW) {
+        const int src = sm.order[k];
+        for (int c = lane; c < n; c += 32)
+            tg[(size_t)k * n + c] = t_old ? t_old[(size_t)src * n + c] : (src == c ? T(1) : T(0));
     }
     __syncthreads();
-    form_q_cm_t<T>(u_new, s, sm.tau, n);
-    __syncthreads();
-    for (int k = warp_id(); k < n; k += kNW)
-        for (int i = lane; i <= k; i += 32) s[(size_t)k * n + i] = s[(size_t)k * n + i] / sm.dv[i];
-    __syncthreads();
-    for (int i = warp_id(); i < n; i += kNW) {
-        for (int c = lane; c < n; c += 32) {
-            T acc = T(0);
-            for (int k = i; k < n; ++k) {
-                const int src = sm.order[k];
-                const T tv = t_old ? t_old[(size_t)src * n + c] : (src == c ? T(1) : T(0));
-                acc = fma((T)s[(size_t)k * n + i], tv, acc);
-            }
-            t_new[(size_t)i * n + c] = acc;
-        }
+    {
+        GemmOpt<T> o;
+        o.rs = sm.xt[0];
+        gemm_t<T, EMU, true, false>(sm, t_new, n, (const double*)s, n, (const T*)tg, n, n, n, n, o);
     }
     __syncthreads();
     if (threadIdx.x == 0) sm.sub[1] += clock64() - t1;
@@ -549,7 +619,7 @@ __device__ void right_stack_t(const ChainDesc& d, TSmem<T>& sm, int s, double* l
             }
             T* t = za; za = zb; zb = t;
         }
-        const double sg = udt_absorb_t<T>(d, sm, za, c ? slot_d(sm, prev, nn) : nullptr,
+        const double sg = udt_absorb_t<T, EMU>(d, sm, za, c ? slot_d(sm, prev, nn) : nullptr,
                                           c ? slot_T(sm, prev, nn) : nullptr, slot_U(sm, cur, nn),
                                           slot_d(sm, cur, nn), slot_T(sm, cur, nn));
         if (threadIdx.x == 0) slot_d(sm, cur, nn)[n] = sg;
@@ -589,7 +659,7 @@ __device__ void left_step_t(const ChainDesc& d, TSmem<T>& sm, int s, int p_in, b
         gemm_t<T, EMU, true, false>(sm, zb, n, ek, n, za, n, n, n, n);   // e^{-dtau K}^T (e^V Z)
         T* t = za; za = zb; zb = t;
     }
-    const double sg = udt_absorb_t<T>(d, sm, za, first ? nullptr : slot_d(sm, in, nn),
+    const double sg = udt_absorb_t<T, EMU>(d, sm, za, first ? nullptr : slot_d(sm, in, nn),
                                       first ? nullptr : slot_T(sm, in, nn), slot_U(sm, out, nn),
                                       slot_d(sm, out, nn), slot_T(sm, out, nn));
     if (threadIdx.x == 0) slot_d(sm, out, nn)[n] = sg;
