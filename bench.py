@@ -11,9 +11,12 @@ the time per sweep; sweeps/s is reported beside it.  Inputs are synthetic random
 Workload square16_beta8 (default; the configuration the metric "batched mixed vs plain
 FP64 at max|dG| <= 1e-6" is quoted on): 64 chains of 16x16 (N=256), U=4, beta=8, dtau=0.1
 (L=80), dqmc, stabilisation every 8 slices, on-device Philox uniforms.  `value` is the
-float64 engine (the only one meeting the max|dG| bar); the mixed-precision engine's
-throughput, speed-up and measured max|dG| against float64 on identical inputs are in
-`mixed`.
+batched mixed-precision engine that meets the max|dG| <= 1e-6 bar: precision "fp64e", every
+dense product (wraps, B-chain, delayed rank-k updates, the blocked QR's and the LU's
+updates) a float64-accurate GEMM emulated on the tcgen05 BF16 tensor cores, the per-site
+updates and panel factorisations in float64.  `fp64` carries the plain float64 engine on
+the same workload (throughput and the speed-up of `value` over it) and `fp32_mixed` the
+float32 engine; both carry max|dG| against float64 on identical fields and uniforms.
 
 Workload batched_fp64: 512 chains, 128 each of 4x4, 6x6, 8x8, 10x10, U drawn per chain
 from {2, 4, 6}, beta=4, L=40, dqmc float64, stabilisation every 5 slices.
@@ -22,10 +25,13 @@ value      device throughput with all state resident in HBM.
 e2e        the same sweeps through the public C ABI in replay mode (the drop-in path of
            LatticeQMC._update_step): each step uploads that sweep's uniforms from pinned
            host memory and downloads every chain's G, copies inside the timed region.
-roofline   the sweep kernel against the measured float64 throughput of this GPU (cuBLAS
-           DGEMM, timed here); algorithmic flops per sweep and chain
-           8 L N^3 (wraps) + 4 L N^3 (B-chain) + 2 (L / n_s) (4/3) N^3 (QR) + 4 A N^2
-           (A = accepted flips, counted on the device).
+roofline   algorithmic float64 flops per sweep and chain
+           F = 8 L N^3 (wraps) + 4 L N^3 (B-chain) + 2 (L / n_s) (4/3) N^3 (QR) + 4 A N^2
+           (A = accepted flips, counted on the device).  fp64e engine: bound "tensor",
+           achieved = 36 F / sweep time (each float64 product is 36 BF16 slice products),
+           peak = the measured sustained BF16 rate (MEASURED_PEAKS.json); `fp64_equivalent`
+           gives F / time against the float64 DGEMM rate measured here.  batched_fp64
+           workload: F / time against that DGEMM rate.
 cpu_baseline  the reference's fast sweep restated in Python/numpy (oracle/compat.py, with
            the pure-Python rank-1 loop of lqmc.py:328-331) on a bounded sample of every
            lattice size of the workload, one process per host core.
@@ -91,7 +97,7 @@ def workload_square16(rank=0, chains=64):
     cfg = {"workload": f"square16_beta8: {chains} chains of 16x16 periodic (N=256), U=4, mu=0, "
                        "beta=8, dtau=0.1 (L=80), dqmc, stab every 8, philox",
            "chains": chains, "sides": [side], "beta": beta, "L": L, "stab_every": 8,
-           "precision": "fp64 (value) and mixed (reported in `mixed`)", "mode": "dqmc"}
+           "precision": "fp64e (value); fp64 and fp32 mixed reported beside it", "mode": "dqmc"}
     return specs, cfg
 
 
@@ -283,20 +289,22 @@ def time_engine(torch, specs, precision, stab, steps, warmup, stream, seed, dev,
     accepted = [(dg["accepted"] - a) / steps for a, dg in zip(acc0, diags)]
     out = dict(ms=ms, launches=launches, clocks=clk, accepted=accepted,
                resid=max(dg["max_residual"] for dg in diags),
-               status_bad=int(np.count_nonzero(eng.status() & 3)),
+               status_bad=int(np.count_nonzero(eng.status() & 11)),
                phases={k: float(np.mean([dg["phase_cycles"][k] for dg in diags]))
-                       for k in diags[0]["phase_cycles"]})
+                       for k in diags[0]["phase_cycles"]},
+               subs={k: float(np.mean([dg["sub_cycles"][k] for dg in diags]))
+                     for k in diags[0]["sub_cycles"]})
     eng.close()
     return out
 
 
-def green_difference(specs, stab, dev, sweeps=1):
-    """max|G_mixed - G_fp64| after `sweeps` sweeps from identical fields and uniforms."""
+def green_difference(specs, stab, dev, precision, sweeps=1):
+    """max|G_precision - G_fp64| after `sweeps` sweeps from identical fields and uniforms."""
     from latticeqmc_gb300 import Engine
     rng = np.random.default_rng(77)
     a = Engine(specs, mode="dqmc", precision="fp64", rng="replay", stab_every=stab, device=dev,
                record=True)
-    b = Engine(specs, mode="dqmc", precision="mixed", rng="replay", stab_every=stab, device=dev,
+    b = Engine(specs, mode="dqmc", precision=precision, rng="replay", stab_every=stab, device=dev,
                record=True)
     total = sum(c.n * c.L for c in specs)
     for _ in range(sweeps):
@@ -321,9 +329,9 @@ def green_difference(specs, stab, dev, sweeps=1):
                 chains_with_identical_decisions=int(sum(same)), chains=len(specs))
 
 
-def time_e2e(torch, specs, stab, steps, warmup, stream, dev, world, rank):
+def time_e2e(torch, specs, stab, steps, warmup, stream, dev, world, rank, precision):
     from latticeqmc_gb300 import Engine
-    eng = Engine(specs, mode="dqmc", rng="replay", stab_every=stab, device=dev)
+    eng = Engine(specs, mode="dqmc", precision=precision, rng="replay", stab_every=stab, device=dev)
     total_uni = sum(c.n * c.L for c in specs)
     total_g = sum(2 * c.n * c.n for c in specs)
     steps_all = warmup + steps
@@ -364,21 +372,31 @@ def run_ours(args, rank, world):
     stab = cfg["stab_every"]
     stream = torch.cuda.Stream()
     seed = 12345 + 1000003 * rank
-    main = time_engine(torch, specs, "fp64", stab, args.steps, args.warmup, stream, seed, dev,
+    headline = "fp64e" if args.workload == "square16_beta8" else "fp64"
+    main = time_engine(torch, specs, headline, stab, args.steps, args.warmup, stream, seed, dev,
                        world, sample_clocks=True)
-    mixed = None
+    others = {}
     if args.workload == "square16_beta8":
-        mx = time_engine(torch, specs, "mixed", stab, args.steps, args.warmup, stream, seed, dev, world)
-        dg = green_difference(specs, stab, dev)
-        mixed = dict(ms_per_step=mx["ms"], status_flagged_chains=mx["status_bad"],
-                     max_stabilisation_residual=mx["resid"], **dg)
-    e2e_ms, h2d, d2h = time_e2e(torch, specs, stab, args.steps, args.warmup, stream, dev, world, rank)
+        dg = green_difference(specs, stab, dev, "fp64e")
+        main.update(dg)
+        for prec, key in (("fp64", "fp64"), ("mixed", "fp32_mixed")):
+            o = time_engine(torch, specs, prec, stab, args.steps, args.warmup, stream, seed, dev, world)
+            od = dict(ms_per_step=o["ms"], status_flagged_chains=o["status_bad"],
+                      max_stabilisation_residual=o["resid"])
+            if prec != "fp64":
+                od.update(green_difference(specs, stab, dev, prec))
+            others[key] = od
+    e2e_ms, h2d, d2h = time_e2e(torch, specs, stab, args.steps, args.warmup, stream, dev, world,
+                                rank, headline)
     peak = fp64_peak_tflops(torch) if rank == 0 else None
     return dict(ms=main["ms"], sites=sum(c.n * c.L for c in specs), chains=len(specs),
                 flops=algorithmic_flops(specs, main["accepted"], stab), launches=main["launches"],
                 clocks=main["clocks"], e2e_ms=e2e_ms, h2d=h2d, d2h=d2h, cfg=cfg,
                 resid=main["resid"], status_bad=main["status_bad"], peak=peak, specs=specs,
-                phases=main["phases"], mixed=mixed)
+                phases=main["phases"], subs=main["subs"], others=others, headline=headline,
+                dg=dict((k, main[k]) for k in ("max_dG", "max_dG_identical_decisions",
+                                               "chains_with_identical_decisions", "chains")
+                        if k in main))
 
 
 def main():
@@ -436,35 +454,63 @@ def main():
         cpu = cpu_baseline(r["specs"], r["cfg"], seconds_per_size=args.cpu_seconds)
         cpu.pop("sweep_seconds", None)
     if rank == 0:
-        achieved = r["flops"] / (r["ms"] * 1e-3) / 1e12
+        fp64_eq = r["flops"] / (r["ms"] * 1e-3) / 1e12
+        if r["headline"] == "fp64e":
+            peaks = {}
+            try:
+                with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                    peaks = json.load(f)
+            except (OSError, ValueError):
+                pass
+            tpeak = peaks.get("bf16_tflops_sustained")
+            tsrc = "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"
+            if tpeak is None:
+                tpeak, tsrc = 1700.0, "fallback sustained bf16 figure (of fallback)"
+            achieved = 36.0 * fp64_eq
+            roof = {"bound": "tensor", "achieved": achieved, "peak": tpeak, "unit": "TFLOP/s",
+                    "frac": achieved / tpeak, "traffic": None, "peak_source": tsrc,
+                    "kernel": "sweep kernel of the fp64e engine (BF16 slice products: 36 per "
+                              "algorithmic float64 flop)",
+                    "fp64_equivalent": {"achieved": fp64_eq, "peak": r["peak"], "unit": "TFLOP/s",
+                                        "frac": fp64_eq / r["peak"] if r["peak"] else None,
+                                        "peak_source": "cuBLAS DGEMM 4096^3 measured in this run"}}
+            dtype = "f64 (GEMMs emulated: 8 BF16 slices, FP32 tensor-core accumulation)"
+        else:
+            roof = {"bound": "fp64", "achieved": fp64_eq, "peak": r["peak"], "unit": "TFLOP/s",
+                    "frac": fp64_eq / r["peak"] if r["peak"] else None, "traffic": None,
+                    "peak_source": "cuBLAS DGEMM 4096^3 measured in this run "
+                                   "(MEASURED_PEAKS.json carries no float64 figure)",
+                    "kernel": "sweep kernel of the float64 engine (all launch buckets of one sweep)"}
+            dtype = "f64"
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"],
             "sweeps_per_s": 1e3 / r["ms"], "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "vs_baseline": None, "dtype": dtype, "data": "synthetic",
             "config": dict(r["cfg"], parallelism=f"chains sharded over {world} GPU(s)",
                            l2="working set (per-chain G, GEMM temporaries and UDT stacks; "
                               "0.6-1.6 GB) exceeds the 129 MB L2; no flush"),
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"]},
             "gpu_launches": r["launches"],
-            "roofline": {"bound": "fp64", "achieved": achieved, "peak": r["peak"],
-                         "unit": "TFLOP/s", "frac": achieved / r["peak"] if r["peak"] else None,
-                         "traffic": None,
-                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run "
-                                        "(MEASURED_PEAKS.json carries no float64 figure)",
-                         "kernel": "sweep kernel of the float64 engine (all launch buckets of one sweep)"},
+            "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": r["clocks"],
-            "accuracy": {"max_stabilisation_residual": r["resid"],
-                         "chains_with_status_flags": r["status_bad"]},
+            "accuracy": dict({"max_stabilisation_residual": r["resid"],
+                              "chains_with_status_flags": r["status_bad"]}, **r["dg"]),
             "phase_share": {k: v / max(sum(r["phases"].values()), 1.0) for k, v in r["phases"].items()},
+            "sub_share": {k: v / max(sum(r["phases"].values()), 1.0) for k, v in r["subs"].items()},
         }
-        if r["mixed"]:
-            mx = r["mixed"]
-            line["mixed"] = dict(mx, value=sites_all / (mx["ms_per_step"] * 1e-3), unit=UNIT,
-                                 speedup_vs_fp64=r["ms"] / mx["ms_per_step"])
-            line["mixed"]["meets_max_dG_1e-6"] = bool(mx["max_dG"] <= 1e-6)
+        if "max_dG" in r["dg"]:
+            line["accuracy"]["meets_max_dG_1e-6"] = bool(r["dg"]["max_dG"] <= 1e-6)
+        for key, od in r["others"].items():
+            entry = dict(od, value=sites_all / (od["ms_per_step"] * 1e-3), unit=UNIT)
+            if key == "fp64":
+                entry["speedup_of_value"] = od["ms_per_step"] / r["ms"]
+            else:
+                entry["speedup_vs_fp64"] = r["others"]["fp64"]["ms_per_step"] / od["ms_per_step"]
+                entry["meets_max_dG_1e-6"] = bool(od["max_dG"] <= 1e-6)
+            line[key] = entry
         print(json.dumps(line))
     if world > 1:
         import torch

@@ -50,9 +50,9 @@ extern "C" {
 #define LQMC_PREC_FP64 0     /* every floating-point operation in float64                */
 #define LQMC_PREC_MIXED 1    /* float32 G, wraps and delayed updates; FP64 stabilisation */
 #define LQMC_PREC_FP64E 2    /* float64 G and updates; every dense product a float64-accurate
-                                GEMM emulated on the tcgen05 BF16 tensor cores (48-bit sliced
-                                operands, exact FP32 accumulation in tensor memory); FP64
-                                Householder QR                                               */
+                                GEMM emulated on the tcgen05 BF16 tensor cores (operands as
+                                56-bit fixed point in 8 balanced base-128 digits, exact FP32
+                                accumulation in tensor memory); FP64 Householder panels     */
 
 /* uniform-draw sources */
 #define LQMC_RNG_REPLAY 0    /* caller uploads the uniforms (e.g. numpy's stream)        */
@@ -100,8 +100,18 @@ typedef struct lqmc_params {
     int32_t device;        /* CUDA device ordinal                                          */
     int32_t engine;        /* LQMC_ENGINE_*: which sweep kernel runs the chains            */
     int32_t debug;         /* LQMC_DEBUG_* bits; 0 in production                           */
-    int32_t reserved[5];
+    int32_t fp64e_native;  /* LQMC_FP64E_NATIVE_* bits: product categories the fp64e engine
+                              keeps in native float64 (0: all on the tensor cores)            */
+    int32_t reserved[4];
 } lqmc_params;
+
+/* product categories of the fp64e engine (lqmc_params.fp64e_native); the LU of the stabilised
+ * inverse is always native float64 */
+#define LQMC_FP64E_NATIVE_WRAP 1     /* the two products of every slice wrap                  */
+#define LQMC_FP64E_NATIVE_STACK 2    /* B-chain products of the UDT stacks                    */
+#define LQMC_FP64E_NATIVE_UDT 4      /* blocked QR updates, Q and T of the UDT factors        */
+#define LQMC_FP64E_NATIVE_GREEN 8    /* U_R^T U_L, T_R T_L^T and U_L Z of the stable inverse   */
+#define LQMC_FP64E_NATIVE_UPDATE 16  /* delayed rank-k updates G -= X Y^T                     */
 
 /* debug bits (lqmc_params.debug), for testing the failure paths */
 #define LQMC_DEBUG_STALL_TC_WAIT 1  /* emulated-GEMM kernel: the first tensor-core step issues

@@ -21,6 +21,7 @@ RNGS = {"replay": 0, "philox": 1}
 ENGINES = {"auto": 0, "smem": 1, "tiled": 2}
 STATUS_NONFINITE, STATUS_SINGULAR, STATUS_DRIFT, STATUS_TIMEOUT = 1, 2, 4, 8
 DEBUG_STALL_TC_WAIT = 1
+FP64E_NATIVE = {"wrap": 1, "stack": 2, "udt": 4, "green": 8, "update": 16}
 OBS_HEADER = 8
 DIAG_LEN = 24
 
@@ -33,7 +34,8 @@ class Params(ctypes.Structure):
     _fields_ = [("mode", ctypes.c_int32), ("precision", ctypes.c_int32), ("rng", ctypes.c_int32),
                 ("stab_every", ctypes.c_int32), ("delay", ctypes.c_int32), ("record", ctypes.c_int32),
                 ("seed", ctypes.c_uint64), ("device", ctypes.c_int32), ("engine", ctypes.c_int32),
-                ("debug", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+                ("debug", ctypes.c_int32), ("fp64e_native", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 4)]
 
 
 class LqmcError(RuntimeError):
@@ -98,12 +100,20 @@ class Handle:
     """Owns one lqmc_handle; every call checks the return code."""
 
     def __init__(self, mode, precision, rng, stab_every, delay, seed, record, device,
-                 engine="auto", debug=0):
+                 engine="auto", debug=0, fp64e_native=()):
         self.lib = load()
+        if isinstance(fp64e_native, int):
+            native = fp64e_native
+        else:
+            native = 0
+            for name in fp64e_native:
+                if name not in FP64E_NATIVE:
+                    raise ValueError(f"unknown fp64e product category {name!r}")
+                native |= FP64E_NATIVE[name]
         p = Params(mode=MODES[mode], precision=PRECISIONS[precision], rng=RNGS[rng],
                    stab_every=int(stab_every), delay=int(delay), record=int(bool(record)),
                    seed=int(seed) & ((1 << 64) - 1), device=int(device), engine=ENGINES[engine],
-                   debug=int(debug))
+                   debug=int(debug), fp64e_native=int(native))
         h = ctypes.c_void_p()
         rc = self.lib.lqmc_create(ctypes.byref(p), ctypes.byref(h))
         if rc != LQMC_OK:

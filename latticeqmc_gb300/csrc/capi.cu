@@ -244,6 +244,7 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
         d.u = u[c];
         d.drift_tol = 1e-6;
         d.debug = h->p.debug;
+        d.native = h->p.fp64e_native;
         if (h->p.precision == LQMC_PREC_MIXED) kind[c] = kTiledFp32;
         else if (h->p.precision == LQMC_PREC_FP64E) kind[c] = kTiledFp64e;
         else if (h->p.engine == LQMC_ENGINE_TILED) kind[c] = kTiledFp64;

@@ -44,7 +44,7 @@ struct ChainDesc {
     int32_t delay;            // tiled kernel: rank-k depth of the delayed updates (>= 1)
     int32_t oz_stages;        // tiled kernel, emulated GEMMs: tensor-core stage buffers (1 or 2)
     int32_t debug;            // LQMC_DEBUG_* bits
-    int32_t pad1;
+    int32_t native;           // LQMC_FP64E_NATIVE_* bits (emulated-GEMM kernel)
 };
 
 }  // namespace lqmc

@@ -2,17 +2,19 @@
 // blk::kNT threads (Ozaki-style operand splitting, exact integer slice products).
 //
 // Row i of op(A) is scaled by 2^-E_i (E_i = exponent just above its largest entry) and
-// written as a 48-bit fixed-point integer F = trunc(|a| 2^(48 - E_i)) cut into kSlices = 8
-// six-bit slices q_t in [-63, 63] (exact in bfloat16); columns of op(B) likewise with 2^-F_j.
-// Then C_ij = 2^(E_i + F_j - 54) sum_{d<8} 2^(6 (7 - d)) D_d with D_d = sum_{t+u=d} (A_t B_u)_ij,
-// keeping the 36 leading slice pairs.  Each A_t B_u is a tcgen05.mma (kind::f16, BF16 x BF16
-// -> FP32, M = 128, K = 16) accumulating into the TMEM columns of diagonal d, so the eight
+// rounded to the nearest 55-bit fixed-point integer N = round(a 2^(55 - E_i)), |N| <= 2^55,
+// which is written in kSlices = 8 balanced base-128 digits q_t in [-64, 64] (exact in
+// bfloat16): N = sum_t q_t 2^(7 (7 - t)).  Columns of op(B) likewise with 2^-F_j.  Then
+// C_ij = 2^(E_i + F_j - 61) sum_{d<8} 2^(7 (7 - d)) D_d with D_d = sum_{t+u=d} (A_t B_u)_ij,
+// keeping the 36 leading digit pairs.  The operands carry 2^-56 of their row / column
+// maximum, finer than float64's own rounding, and the rounding and the dropped pairs
+// (t + u >= 8, below 2^-60) have either sign, so their errors do not accumulate
+// systematically over k.  Each A_t B_u is a tcgen05.mma (kind::f16, BF16 x BF16 -> FP32,
+// M = 128, K = 16) accumulating into the TMEM columns of diagonal d, so the eight
 // accumulators of a 128 x 64 output tile fill the 512 TMEM columns.  The FP32 sums are exact
-// integers while |D_d| <= 8 k 63^2 < 2^24, i.e. for k <= kMaxK = 512; longer products are
-// cut into chunks of kMaxK whose results are added in float64.  The only roundings are the
-// truncation of the operands at 2^-48 of their row / column maximum and the final
-// conversion to float64.  A row (column) holding a NaN or Inf gives NaN in its output row
-// (column).
+// integers while |D_d| <= 8 k 64^2 <= 2^24, i.e. for k <= kMaxK = 512; longer products are cut
+// into chunks of kMaxK whose results are added in float64.  A row (column) holding a NaN or
+// Inf gives NaN in its output row (column).
 //
 // Data movement: the split writes every slice directly in the tensor core's canonical
 // K-major, no-swizzle layout (8 x 16-byte core matrices), grouped so that all eight slices
@@ -39,8 +41,8 @@ namespace ozt {
 using namespace blk;
 
 constexpr int kSlices = 8;
-constexpr int kBits = 6;
-constexpr int kWidth = kSlices * kBits;
+constexpr int kBits = 7;
+constexpr int kWidth = kSlices * kBits - 1;   // 55: the top digit absorbs the rounding carry
 constexpr int kBM = 128, kBN = 64, kBK = 16;
 constexpr int kTileA = kBM * kBK;             // bf16 elements of one slice tile of A (4 KB)
 constexpr int kTileB = kBN * kBK;             // one slice tile of B (2 KB)
@@ -143,15 +145,18 @@ __device__ __forceinline__ bool bar_wait(unsigned long long* bar, uint32_t parit
 
 // ---- splitting ---------------------------------------------------------------------------
 
-// 48-bit fixed-point magnitude of v for exponent e (|v| < 2^e), 0 for zero / non-finite
-__device__ __forceinline__ unsigned long long fixed48(double v, int e) {
+// N = round(v 2^(55 - e)) for |v| < 2^e (ties away from zero), 0 for zero / non-finite
+__device__ __forceinline__ long long fixed55(double v, int e) {
     const long long bits = __double_as_longlong(v);
     const int be = (int)((bits >> 52) & 0x7FF);
     if (be == 0 || be == 0x7FF || e == kNonFinite) return 0;
     const unsigned long long mant = ((unsigned long long)bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh = (be - 1075) + kWidth - e;
-    if (sh >= 0) return (sh < 11) ? (mant << sh) : 0;
-    return (-sh < 64) ? (mant >> (-sh)) : 0;
+    // v 2^(55 - e) = mant 2^(be - 1075 + 55 - e); |v| < 2^e bounds the left shift by 2
+    const int rs = 1075 - 55 + e - be;
+    unsigned long long mag;
+    if (rs <= 0) mag = mant << (-rs);
+    else mag = (rs < 64) ? ((mant >> (rs - 1)) + 1ull) >> 1 : 0ull;
+    return bits < 0 ? -(long long)mag : (long long)mag;
 }
 
 // Split X (rows x k), X(r, q) = trans ? x[q ld + r] : x[r ld + q], into the tile layout with
@@ -205,34 +210,44 @@ __device__ void split_tiles(const double* x, int ld, bool trans, int rows, int k
     for (int u = threadIdx.x; u < rp * groups; u += kNT) {
         const int r = u % rp, g = u / rp, q0 = g * 8;
         const int e = (r < rows) ? exps[r] : 0;
-        // 48-bit magnitudes as two 24-bit halves (slices 0-3 and 4-7), sign masks per pair
-        uint32_t fh[8], fl[8], sgn[4];
+        // balanced digits: the low 28 bits give digits 7..4 and a carry into the high part,
+        // which gives digits 3..0 (all in 32-bit integers); q_t in [-64, 64]
+        constexpr int kHalf = kBits * kSlices / 2, kRadix = 1 << kBits;
+        int dg[kSlices][8];
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
             const int q = q0 + c;
             double v = 0.0;
             if (r < rows && q < k) v = trans ? x[(size_t)q * ld + r] : x[(size_t)r * ld + q];
-            const unsigned long long f = fixed48(v, e);
-            fh[c] = (uint32_t)(f >> 24);
-            fl[c] = (uint32_t)f & 0xFFFFFFu;
-            if (c & 1) sgn[c >> 1] |= (__double_as_longlong(v) < 0) ? 0x80000000u : 0u;
-            else sgn[c >> 1] = (__double_as_longlong(v) < 0) ? 0x8000u : 0u;
+            const long long nf = fixed55(v, e);
+            int lo = (int)(nf & ((1ll << kHalf) - 1)), hi = (int)(nf >> kHalf);
+#pragma unroll
+            for (int t = kSlices - 1; t >= kSlices / 2; --t) {
+                const int dd = ((lo + kRadix / 2) & (kRadix - 1)) - kRadix / 2;
+                dg[t][c] = dd;
+                lo = (lo - dd) >> kBits;
+            }
+            hi += lo;   // carry out of the low half: 0 or 1
+#pragma unroll
+            for (int t = kSlices / 2 - 1; t > 0; --t) {
+                const int dd = ((hi + kRadix / 2) & (kRadix - 1)) - kRadix / 2;
+                dg[t][c] = dd;
+                hi = (hi - dd) >> kBits;
+            }
+            dg[0][c] = hi;
         }
         const int rb = r / BLK, rr = r % BLK, s = q0 / kBK;
         __nv_bfloat16* base = dst + ((size_t)(rb * S + s) * kSlices) * (BLK * kBK) + core_offset(rr, q0 % kBK);
 #pragma unroll
         for (int t = 0; t < kSlices; ++t) {
-            const int sh = kBits * (kSlices / 2 - 1 - (t & 3));
             uint32_t w[4];
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
-                const uint32_t a0 = ((t < 4 ? fh[2 * c] : fl[2 * c]) >> sh) & 63u;
-                const uint32_t a1 = ((t < 4 ? fh[2 * c + 1] : fl[2 * c + 1]) >> sh) & 63u;
-                // small integers are exact in float (2^23 magic) and in bfloat16
-                const float f0 = __uint_as_float(0x4B000000u | a0) - 8388608.0f;
-                const float f1 = __uint_as_float(0x4B000000u | a1) - 8388608.0f;
+                // small signed integers are exact in float (1.5 2^23 magic) and in bfloat16
+                const float f0 = __int_as_float(0x4B400000 + dg[t][2 * c]) - 12582912.0f;
+                const float f1 = __int_as_float(0x4B400000 + dg[t][2 * c + 1]) - 12582912.0f;
                 const __nv_bfloat162 p = __floats2bfloat162_rn(f0, f1);
-                w[c] = *reinterpret_cast<const uint32_t*>(&p) | sgn[c];
+                w[c] = *reinterpret_cast<const uint32_t*>(&p);
             }
             *reinterpret_cast<uint4*>(base + (size_t)t * (BLK * kBK)) = make_uint4(w[0], w[1], w[2], w[3]);
         }
@@ -438,19 +453,21 @@ __device__ void oz_gemm_tc(double* c, int ldc, const double* a, int lda, const d
                     tmem_wait();
 #pragma unroll
                     for (int x = 0; x < 8; ++x) {
-                        // T = sum_d D_d 2^(6 (7 - d)) / 16 by Horner: |D_d| < 2^24 is exact in
-                        // int32 (D_0 64 + D_1 < 2^31), |T| < 2^63; dropping the low 4 bits of D_7
-                        // is far below the 2^-48 truncation of the operands
+                        // T = sum_d D_d 2^(7 (7 - d)) / 2^12 from two Horner halves (|D_d| <= 2^24,
+                        // each half < 2^46); the 12 dropped low bits are 2^-60 of the largest sum
                         int q[kSlices];
 #pragma unroll
                         for (int d = 0; d < kSlices; ++d) q[d] = __float2int_rn(__uint_as_float(r[d][x]));
-                        long long t = (long long)(q[0] * 64 + q[1]);
+                        long long hi = q[0], lo = q[kSlices / 2];
 #pragma unroll
-                        for (int d = 2; d < kSlices - 1; ++d) t = t * 64 + q[d];
-                        t = t * 4 + (q[kSlices - 1] >> 4);
-                        // C = T 2^(E_i + F_j - 2W + 6 (S - 1) + 4)
+                        for (int d = 1; d < kSlices / 2; ++d) {
+                            hi = hi * (1 << kBits) + q[d];
+                            lo = lo * (1 << kBits) + q[kSlices / 2 + d];
+                        }
+                        const long long t = hi * (1ll << (kBits * kSlices / 2 - 12)) + (lo >> 12);
+                        // C = T 2^(E_i + F_j - 2W + 7 (S - 1) + 12)
                         double v = 0.0;
-                        if (t != 0) v = scaled_double(t, ei + ej[x] - 2 * kWidth + kBits * (kSlices - 1) + 4);
+                        if (t != 0) v = scaled_double(t, ei + ej[x] - 2 * kWidth + kBits * (kSlices - 1) + 12);
                         if (ei == kNonFinite || ej[x] == kNonFinite) v = __longlong_as_double(0x7FF8000000000000ll);
                         ts[row * kTs + cl + x] = v;
                     }

@@ -88,6 +88,7 @@ struct TSmem {
     double* panel;    // blocked LU panel, n x (panel_width + 1); overlays stage, dx, dy
     int* piv;         // [kPanel] panel pivots
     double* stage64;  // float64 GEMM staging of the LU (float kernel; same region as stage)
+    int native;       // LQMC_FP64E_NATIVE_* categories kept in native float64 (EMU kernel)
 };
 
 template <typename T> __device__ __forceinline__ T* slot_U(const TSmem<T>& sm, int idx, size_t nn) {
@@ -101,13 +102,15 @@ template <typename T> __device__ __forceinline__ double* slot_d(const TSmem<T>& 
 }
 
 // Dense product of the tiled kernel: the block-tiled SIMT GEMM, or with EMU the float64
-// GEMM emulated on the tcgen05 BF16 tensor cores (ozaki_tc.cuh).
-template <typename T, bool EMU, bool TA, bool TB, typename TAIn, typename TBIn>
+// GEMM emulated on the tcgen05 BF16 tensor cores (ozaki_tc.cuh), unless the product's
+// category (LQMC_FP64E_NATIVE_* bit) is kept in native float64 for this chain.
+template <typename T, bool EMU, int Cat, bool TA, bool TB, typename TAIn, typename TBIn>
 __device__ __forceinline__ void gemm_t(TSmem<T>& sm, T* c, int ldc, const TAIn* a, int lda,
                                        const TBIn* b, int ldb, int m, int n, int k,
                                        GemmOpt<T> o = GemmOpt<T>()) {
     if constexpr (EMU) {
-        ozt::oz_gemm_tc<TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.oz, o);
+        if (sm.native & Cat) tile_gemm<T, TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.stage64, o);
+        else ozt::oz_gemm_tc<TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.oz, o);
     } else {
         tile_gemm<T, TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.stage, o);
     }
@@ -338,10 +341,10 @@ __device__ void lu_solve_blocked(TSmem<double>& sm, double* w, double* rhs, int 
             GemmOpt<double> o;
             o.subtract = true;
             // W22 -= L21 U12 ; R2 -= L21 R1
-            gemm_t<double, EMU, false, false>(sm, w + (size_t)(jb + nb) * n + jb + nb, n,
+            gemm_t<double, EMU, 0, false, false>(sm, w + (size_t)(jb + nb) * n + jb + nb, n,
                                               w + (size_t)(jb + nb) * n + jb, n,
                                               w + (size_t)jb * n + jb + nb, n, rest, rest, nb, o);
-            gemm_t<double, EMU, false, false>(sm, rhs + (size_t)(jb + nb) * n, n,
+            gemm_t<double, EMU, 0, false, false>(sm, rhs + (size_t)(jb + nb) * n, n,
                                               w + (size_t)(jb + nb) * n + jb, n,
                                               rhs + (size_t)jb * n, n, rest, n, nb, o);
         }
@@ -364,7 +367,7 @@ __device__ void lu_solve_blocked(TSmem<double>& sm, double* w, double* rhs, int 
             GemmOpt<double> o;
             o.subtract = true;
             // R0 -= U01 R1
-            gemm_t<double, EMU, false, false>(sm, rhs, n, w + jb, n, rhs + (size_t)jb * n, n, jb, n, nb, o);
+            gemm_t<double, EMU, 0, false, false>(sm, rhs, n, w + jb, n, rhs + (size_t)jb * n, n, jb, n, nb, o);
         }
     }
     *logabs = la;
@@ -382,9 +385,13 @@ template <>
 __device__ void lu_solve_dispatch<double, false>(TSmem<double>& sm, int n, double* la, double* sw, int* sing) {
     lu_solve_blocked<false>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
 }
+// The emulated kernel keeps the LU's trailing updates in native float64: the stabilised
+// matrix is graded in its rows and columns, so L21 and U12 can carry opposite grading along
+// the contraction index, where an emulated product (accurate relative to the row / column
+// maxima of its operands) would lose the small terms' relative accuracy.
 template <>
 __device__ void lu_solve_dispatch<double, true>(TSmem<double>& sm, int n, double* la, double* sw, int* sing) {
-    lu_solve_blocked<true>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
+    lu_solve_blocked<false>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
 }
 template <>
 __device__ void lu_solve_dispatch<float, false>(TSmem<float>& sm, int n, double* la, double* sw, int* sing) {
@@ -401,8 +408,12 @@ template <typename T, bool EMU, bool TA, bool TB>
 __device__ __forceinline__ void gemm64(TSmem<T>& sm, double* c, int ldc, const double* a, int lda,
                                        const double* b, int ldb, int m, int n, int k,
                                        GemmOpt<double> o = GemmOpt<double>()) {
-    if constexpr (EMU) ozt::oz_gemm_tc<TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.oz, o);
-    else tile_gemm<double, TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.stage64, o);
+    if constexpr (EMU) {
+        if (sm.native & LQMC_FP64E_NATIVE_UDT) tile_gemm<double, TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.stage64, o);
+        else ozt::oz_gemm_tc<TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.oz, o);
+    } else {
+        tile_gemm<double, TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.stage64, o);
+    }
 }
 
 // UDT of Z diag(d_old) T_old (pre-pivoted QR, QR in float64).  z row-major; U is written
@@ -486,10 +497,10 @@ __device__ double udt_absorb_t(const ChainDesc& d, TSmem<T>& sm, const T* z, con
         panel_v(vbuf, s, n, jb, b);
         gemm64<T, EMU, true, false>(sm, ubuf, b, vbuf, rows, tstore + (size_t)p * bw * bw, b, rows, b, b);
         T* q2 = u_new + (size_t)jb * n + jb;
-        gemm_t<T, EMU, false, true>(sm, yq, rows, vbuf, rows, q2, n, b, rows, rows);
+        gemm_t<T, EMU, LQMC_FP64E_NATIVE_UDT, false, true>(sm, yq, rows, vbuf, rows, q2, n, b, rows, rows);
         GemmOpt<T> o;
         o.subtract = true;
-        gemm_t<T, EMU, true, true>(sm, q2, n, yq, rows, (const double*)ubuf, b, rows, rows, b, o);
+        gemm_t<T, EMU, LQMC_FP64E_NATIVE_UDT, true, true>(sm, q2, n, yq, rows, (const double*)ubuf, b, rows, rows, b, o);
     }
     // T_new = diag(1 / d) R (P^T T_old): R's strict lower part (the reflectors) cleared, the
     // rows of T_old gathered in the pivot order
@@ -505,7 +516,7 @@ __device__ double udt_absorb_t(const ChainDesc& d, TSmem<T>& sm, const T* z, con
     {
         GemmOpt<T> o;
         o.rs = sm.xt[0];
-        gemm_t<T, EMU, true, false>(sm, t_new, n, (const double*)s, n, (const T*)tg, n, n, n, n, o);
+        gemm_t<T, EMU, LQMC_FP64E_NATIVE_UDT, true, false>(sm, t_new, n, (const double*)s, n, (const T*)tg, n, n, n, n, o);
     }
     __syncthreads();
     if (threadIdx.x == 0) sm.sub[1] += clock64() - t1;
@@ -539,8 +550,8 @@ __device__ double green_udt_t(const ChainDesc& d, TSmem<T>& sm, const T* ur, con
     }
     if (ul) {
         // X = U_R^T U_L: A(i,p) = U_R[p][i] = ur[i n + p]; B(p,j) = U_L[p][j] = ul[j n + p]
-        gemm_t<T, EMU, false, true>(sm, sm.z0, n, ur, n, ul, n, n, n, n);
-        gemm_t<T, EMU, false, true>(sm, sm.z1, n, tr, n, tl, n, n, n, n);   // Y = T_R T_L^T
+        gemm_t<T, EMU, LQMC_FP64E_NATIVE_GREEN, false, true>(sm, sm.z0, n, ur, n, ul, n, n, n, n);
+        gemm_t<T, EMU, LQMC_FP64E_NATIVE_GREEN, false, true>(sm, sm.z1, n, tr, n, tl, n, n, n, n);   // Y = T_R T_L^T
     }
     __syncthreads();
     for (int i = warp_id(); i < n; i += kNW)
@@ -564,7 +575,7 @@ __device__ double green_udt_t(const ChainDesc& d, TSmem<T>& sm, const T* ur, con
             for (int j = lane; j < n; j += 32) sm.s1[(size_t)i * n + j] /= dbl[i];
         __syncthreads();
         // G = U_L Z: A(i,p) = U_L[i][p] = ul[p n + i]
-        gemm_t<T, EMU, true, false>(sm, sm.z0, n, ul, n, sm.s1, n, n, n, n);
+        gemm_t<T, EMU, LQMC_FP64E_NATIVE_GREEN, true, false>(sm, sm.z0, n, ul, n, sm.s1, n, n, n, n);
         for (int i = warp_id(); i < n; i += kNW)
             for (int j = lane; j < n; j += 32) {
                 const size_t e = (size_t)i * n + j;
@@ -613,9 +624,9 @@ __device__ void right_stack_t(const ChainDesc& d, TSmem<T>& sm, int s, double* l
                 __syncthreads();
             } else if (l == lo) {
                 // B(p, j) = U[p][j] = uc[j n + p] (column-major slot)
-                gemm_t<T, EMU, false, true>(sm, zb, n, ek, n, slot_U(sm, prev, nn), n, n, n, n, o);
+                gemm_t<T, EMU, LQMC_FP64E_NATIVE_STACK, false, true>(sm, zb, n, ek, n, slot_U(sm, prev, nn), n, n, n, n, o);
             } else {
-                gemm_t<T, EMU, false, false>(sm, zb, n, ek, n, za, n, n, n, n, o);   // e^V e^{-dtau K} Z
+                gemm_t<T, EMU, LQMC_FP64E_NATIVE_STACK, false, false>(sm, zb, n, ek, n, za, n, n, n, n, o);   // e^V e^{-dtau K} Z
             }
             T* t = za; za = zb; zb = t;
         }
@@ -656,7 +667,7 @@ __device__ void left_step_t(const ChainDesc& d, TSmem<T>& sm, int s, int p_in, b
                 for (int j = lane; j < n; j += 32)
                     za[(size_t)i * n + j] = sm.ev_t[i] * za[(size_t)i * n + j];
         }
-        gemm_t<T, EMU, true, false>(sm, zb, n, ek, n, za, n, n, n, n);   // e^{-dtau K}^T (e^V Z)
+        gemm_t<T, EMU, LQMC_FP64E_NATIVE_STACK, true, false>(sm, zb, n, ek, n, za, n, n, n, n);   // e^{-dtau K}^T (e^V Z)
         T* t = za; za = zb; zb = t;
     }
     const double sg = udt_absorb_t<T, EMU>(d, sm, za, first ? nullptr : slot_d(sm, in, nn),
@@ -676,8 +687,8 @@ __device__ void wrap_t(const ChainDesc& d, TSmem<T>& sm, int l) {
         for (int j = lane_id(); j < n; j += 32) g[(size_t)i * n + j] *= sm.iev_t[i];
     GemmOpt<T> o;
     o.cs = sm.ev_t;
-    gemm_t<T, EMU, false, false>(sm, sm.z0, n, mat_expkinv<T>(d), n, g, n, n, n, n, o);
-    gemm_t<T, EMU, false, false>(sm, g, n, sm.z0, n, mat_expk<T>(d), n, n, n, n);
+    gemm_t<T, EMU, LQMC_FP64E_NATIVE_WRAP, false, false>(sm, sm.z0, n, mat_expkinv<T>(d), n, g, n, n, n, n, o);
+    gemm_t<T, EMU, LQMC_FP64E_NATIVE_WRAP, false, false>(sm, g, n, sm.z0, n, mat_expk<T>(d), n, n, n, n);
 }
 
 // Site updates of slice l with delayed rank-k updates (k = d.delay): the accepted flips of
@@ -753,14 +764,14 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int sw, 
         if (++m == kd) {
             GemmOpt<T> o;
             o.subtract = true;
-            gemm_t<T, EMU, false, true>(sm, g, n, sm.dx, ld, sm.dy, ld, n, n, m, o);
+            gemm_t<T, EMU, LQMC_FP64E_NATIVE_UPDATE, false, true>(sm, g, n, sm.dx, ld, sm.dy, ld, n, n, m, o);
             m = 0;
         }
     }
     if (m > 0) {
         GemmOpt<T> o;
         o.subtract = true;
-        gemm_t<T, EMU, false, true>(sm, g, n, sm.dx, ld, sm.dy, ld, n, n, m, o);
+        gemm_t<T, EMU, LQMC_FP64E_NATIVE_UPDATE, false, true>(sm, g, n, sm.dx, ld, sm.dy, ld, n, n, m, o);
     }
     __syncthreads();
 }
@@ -902,6 +913,7 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     sm.stage = reinterpret_cast<T*>(p);
     sm.oz.stage = reinterpret_cast<unsigned char*>(p);
     sm.oz.stages = d.oz_stages;
+    sm.native = d.native;
     sm.oz.tc = &tcs;
     sm.stage64 = p;   // the float64 LU staging (float kernel) shares the staging region
     const size_t stage_region = stage_region_bytes(sizeof(T) == 4, EMU, d.oz_stages);

@@ -80,10 +80,13 @@ class Engine:
     rng        'replay' (uniforms uploaded per sweep) or 'philox' (on device)
     engine     'auto', 'smem' (one CTA per chain, G in shared memory, fp64, N <= 128) or
                'tiled' (matrices in global memory, tiled GEMMs; any N up to 2048)
+    fp64e_native  product categories the fp64e engine keeps in native float64: names from
+               'wrap', 'stack', 'udt', 'green', 'update' (or an LQMC_FP64E_NATIVE_* mask)
     """
 
     def __init__(self, chains, mode="dqmc", precision="fp64", rng="philox", stab_every=None,
-                 delay=0, seed=0, record=False, device=0, engine="auto", debug=0):
+                 delay=0, seed=0, record=False, device=0, engine="auto", debug=0,
+                 fp64e_native=()):
         self.chains = list(chains)
         if stab_every is None:
             stab_every = auto_stab_every(self.chains)
@@ -91,7 +94,7 @@ class Engine:
         self.mode, self.precision, self.rng = mode, precision, rng
         self.record = bool(record)
         self._h = _native.Handle(mode, precision, rng, stab_every, delay, seed, record, device,
-                                 engine, debug)
+                                 engine, debug, fp64e_native)
         n = len(self.chains)
         n_sites = np.array([c.n for c in self.chains], dtype=np.int32)
         n_slices = np.array([c.L for c in self.chains], dtype=np.int32)
