@@ -91,6 +91,13 @@ struct Workspace {
     long long* cycles;       // optional [3]: splitting, whole product loop, its epilogues (thread 0)
 };
 
+// An operand split once and reused (constant matrices): its slices in the tile layout of
+// split_tiles (A: row blocks of kBM, B: column blocks of kBN) and its exponents.
+struct Presplit {
+    const __nv_bfloat16* slices;
+    const int* exps;
+};
+
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
@@ -210,48 +217,51 @@ __device__ void split_tiles(const double* x, int ld, bool trans, int rows, int k
     for (int u = threadIdx.x; u < rp * groups; u += kNT) {
         const int r = u % rp, g = u / rp, q0 = g * 8;
         const int e = (r < rows) ? exps[r] : 0;
-        // balanced digits: the low 28 bits give digits 7..4 and a carry into the high part,
-        // which gives digits 3..0 (all in 32-bit integers); q_t in [-64, 64]
-        constexpr int kHalf = kBits * kSlices / 2, kRadix = 1 << kBits;
-        int dg[kSlices][8];
+        // balanced digits without a carry chain: N + kBias (64 in every base-128 digit) has
+        // the plain 7-bit fields q_t + 64 (the top field, 8 bits, takes q_0 + 64 in [0, 128])
+        constexpr long long kBias = 0x81020408102040ll;
+        uint32_t flo[8], fhi[8];
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
             const int q = q0 + c;
             double v = 0.0;
             if (r < rows && q < k) v = trans ? x[(size_t)q * ld + r] : x[(size_t)r * ld + q];
-            const long long nf = fixed55(v, e);
-            int lo = (int)(nf & ((1ll << kHalf) - 1)), hi = (int)(nf >> kHalf);
-#pragma unroll
-            for (int t = kSlices - 1; t >= kSlices / 2; --t) {
-                const int dd = ((lo + kRadix / 2) & (kRadix - 1)) - kRadix / 2;
-                dg[t][c] = dd;
-                lo = (lo - dd) >> kBits;
-            }
-            hi += lo;   // carry out of the low half: 0 or 1
-#pragma unroll
-            for (int t = kSlices / 2 - 1; t > 0; --t) {
-                const int dd = ((hi + kRadix / 2) & (kRadix - 1)) - kRadix / 2;
-                dg[t][c] = dd;
-                hi = (hi - dd) >> kBits;
-            }
-            dg[0][c] = hi;
+            const unsigned long long mb = (unsigned long long)(fixed55(v, e) + kBias);
+            flo[c] = (uint32_t)(mb & ((1ull << 28) - 1));   // fields of digits 7 .. 4
+            fhi[c] = (uint32_t)(mb >> 28);                  // fields of digits 3 .. 0
         }
         const int rb = r / BLK, rr = r % BLK, s = q0 / kBK;
         __nv_bfloat16* base = dst + ((size_t)(rb * S + s) * kSlices) * (BLK * kBK) + core_offset(rr, q0 % kBK);
 #pragma unroll
         for (int t = 0; t < kSlices; ++t) {
+            const int sh = kBits * (kSlices / 2 - 1 - (t & 3));
+            const uint32_t mask = (t == 0) ? 0xFFu : 0x7Fu;
             uint32_t w[4];
 #pragma unroll
             for (int c = 0; c < 4; ++c) {
-                // small signed integers are exact in float (1.5 2^23 magic) and in bfloat16
-                const float f0 = __int_as_float(0x4B400000 + dg[t][2 * c]) - 12582912.0f;
-                const float f1 = __int_as_float(0x4B400000 + dg[t][2 * c + 1]) - 12582912.0f;
+                const uint32_t a0 = ((t < 4 ? fhi[2 * c] : flo[2 * c]) >> sh) & mask;
+                const uint32_t a1 = ((t < 4 ? fhi[2 * c + 1] : flo[2 * c + 1]) >> sh) & mask;
+                // field - 64 exactly in float (2^23 magic) and in bfloat16
+                const float f0 = __uint_as_float(0x4B000000u | a0) - 8388672.0f;
+                const float f1 = __uint_as_float(0x4B000000u | a1) - 8388672.0f;
                 const __nv_bfloat162 p = __floats2bfloat162_rn(f0, f1);
                 w[c] = *reinterpret_cast<const uint32_t*>(&p);
             }
             *reinterpret_cast<uint4*>(base + (size_t)t * (BLK * kBK)) = make_uint4(w[0], w[1], w[2], w[3]);
         }
     }
+}
+
+// Split a constant operand once: as A (TA: A(i, p) = a[p lda + i]) when as_a, else as B
+// (TB: B(p, j) = b[j ldb + p]), of an (m x k) / (k x n) product; `slices` holds
+// kSlices rows_pad(rows, kBM or kBN) kpad(k) bf16 and `exps` rows ints.  `scratch` is shared
+// memory of at least rows ints.  Ends with the fences the bulk copies need.
+__device__ inline void presplit(const double* x, int ld, bool as_a, bool transposed, int rows, int k,
+                                __nv_bfloat16* slices, int* exps, int* scratch) {
+    if (as_a) split_tiles<kBM>(x, ld, transposed, rows, k, exps, slices, scratch);
+    else split_tiles<kBN>(x, ld, !transposed, rows, k, exps, slices, scratch);
+    asm volatile("fence.proxy.async;\n" ::: "memory");
+    __syncthreads();
 }
 
 // ---- tensor-core issue -------------------------------------------------------------------
@@ -336,9 +346,11 @@ __device__ __forceinline__ double scaled_double(long long t, int s) {
 // C (m x n, ldc) = op(A) op(B) with float64 accuracy; epilogue as blk::tile_gemm (row /
 // column scale, subtract).  A(i, p) = TA ? a[p lda + i] : a[i lda + p];
 // B(p, j) = TB ? b[j ldb + p] : b[p ldb + j].
+// pa / pb: op(A) / op(B) already split (same m, n, k); a / b are then not read.
 template <bool TA, bool TB>
 __device__ void oz_gemm_tc(double* c, int ldc, const double* a, int lda, const double* b, int ldb,
-                           int m, int n, int k, const Workspace& ws, GemmOpt<double> opt = GemmOpt<double>()) {
+                           int m, int n, int k, const Workspace& ws, GemmOpt<double> opt = GemmOpt<double>(),
+                           const Presplit* pa = nullptr, const Presplit* pb = nullptr) {
     Tc* tc = ws.tc;
     // callers may have just written A or B; order earlier generic shared-memory use of the
     // stage before the asynchronous copies into it
@@ -353,12 +365,14 @@ __device__ void oz_gemm_tc(double* c, int ldc, const double* a, int lda, const d
         return;
     }
     const int kp = kpad(k), S = kp / kBK;
-    __nv_bfloat16* sa = ws.slices;
-    __nv_bfloat16* sb = ws.slices + (size_t)kSlices * rows_pad(m, kBM) * kp;
+    const __nv_bfloat16* sa = pa ? pa->slices : ws.slices;
+    const __nv_bfloat16* sb = pb ? pb->slices : ws.slices + (size_t)kSlices * rows_pad(m, kBM) * kp;
+    const int* ea = pa ? pa->exps : ws.ea;
+    const int* eb = pb ? pb->exps : ws.eb;
     const long long t0 = clock64();
     int* scratch = reinterpret_cast<int*>(ws.stage);   // the stage is idle while splitting
-    split_tiles<kBM>(a, lda, TA, m, k, ws.ea, sa, scratch);
-    split_tiles<kBN>(b, ldb, !TB, n, k, ws.eb, sb, scratch);
+    if (!pa) split_tiles<kBM>(a, lda, TA, m, k, ws.ea, ws.slices, scratch);
+    if (!pb) split_tiles<kBN>(b, ldb, !TB, n, k, ws.eb, ws.slices + (size_t)kSlices * rows_pad(m, kBM) * kp, scratch);
     // the slices were written through the generic proxy and are read by bulk copies
     asm volatile("fence.proxy.async;\n" ::: "memory");
     __syncthreads();
@@ -436,7 +450,7 @@ __device__ void oz_gemm_tc(double* c, int ldc, const double* a, int lda, const d
             // transposed through the stage buffer, and written with whole-row coalesced stores
             double* ts = reinterpret_cast<double*>(ws.stage);   // [kBM][kTs]
             constexpr int kTs = 33;
-            const int ei = (i0 + row < m) ? ws.ea[i0 + row] : 0;
+            const int ei = (i0 + row < m) ? ea[i0 + row] : 0;
 #pragma unroll 1
             for (int h = 0; h < 2; ++h) {
 #pragma unroll 1
@@ -445,7 +459,7 @@ __device__ void oz_gemm_tc(double* c, int ldc, const double* a, int lda, const d
                     const int ct = 32 * h + cl;             // column within the tile
                     int ej[8];
 #pragma unroll
-                    for (int x = 0; x < 8; ++x) ej[x] = (j0 + ct + x < n) ? ws.eb[j0 + ct + x] : 0;
+                    for (int x = 0; x < 8; ++x) ej[x] = (j0 + ct + x < n) ? eb[j0 + ct + x] : 0;
                     uint32_t r[kSlices][8];
 #pragma unroll
                     for (int d = 0; d < kSlices; ++d)

@@ -38,7 +38,7 @@ __host__ __device__ constexpr size_t align256(size_t b) { return (b + 255) / 256
 // the UDT slots of both spins.
 template <typename T>
 struct TiledLayout {
-    size_t nn, g, z, s, oz, oz_ea, spin_block, slot, total, g_slots;
+    size_t nn, g, z, s, oz, oz_ea, spin_block, slot, total, g_slots, pre, pre_a, pre_b, pre_e;
     __host__ __device__ TiledLayout(int n, int n_chunks, bool emu = false) {
         nn = (size_t)n * n;
         g = 0;                                              // G of the spin       (T)
@@ -51,7 +51,13 @@ struct TiledLayout {
         spin_block = oz_ea + (emu ? align256(2 * (size_t)n * sizeof(int)) : 0);
         g_slots = 2 * spin_block;
         slot = align256(2 * nn * sizeof(T) + (size_t)(n + 1) * sizeof(double));
-        total = g_slots + (size_t)(2 * n_chunks + 4) * slot;
+        pre = g_slots + (size_t)(2 * n_chunks + 4) * slot;
+        // emulated GEMMs: e^{-dtau K} (as A, and transposed as A), e^{+dtau K} (as A) and
+        // e^{-dtau K} (as B) split once per launch, shared by the chain's two CTAs
+        pre_a = emu ? align256((size_t)ozt::kSlices * ozt::rows_pad(n, ozt::kBM) * ozt::kpad(n) * 2) : 0;
+        pre_b = emu ? align256((size_t)ozt::kSlices * ozt::rows_pad(n, ozt::kBN) * ozt::kpad(n) * 2) : 0;
+        pre_e = pre + 3 * pre_a + pre_b;
+        total = pre_e + (emu ? align256(4 * (size_t)n * sizeof(int)) : 0);
     }
 };
 
@@ -89,7 +95,11 @@ struct TSmem {
     int* piv;         // [kPanel] panel pivots
     double* stage64;  // float64 GEMM staging of the LU (float kernel; same region as stage)
     int native;       // LQMC_FP64E_NATIVE_* categories kept in native float64 (EMU kernel)
+    ozt::Presplit pre[4];   // EMU: e^{-dtau K} as A, its transpose as A, e^{+dtau K} as A,
+                            // e^{-dtau K} as B (indices kPreK, kPreKT, kPreKinv, kPreKB)
 };
+
+enum { kPreK = 0, kPreKT = 1, kPreKinv = 2, kPreKB = 3 };
 
 template <typename T> __device__ __forceinline__ T* slot_U(const TSmem<T>& sm, int idx, size_t nn) {
     return reinterpret_cast<T*>(sm.slots + (size_t)idx * sm.slot_bytes);
@@ -107,10 +117,11 @@ template <typename T> __device__ __forceinline__ double* slot_d(const TSmem<T>& 
 template <typename T, bool EMU, int Cat, bool TA, bool TB, typename TAIn, typename TBIn>
 __device__ __forceinline__ void gemm_t(TSmem<T>& sm, T* c, int ldc, const TAIn* a, int lda,
                                        const TBIn* b, int ldb, int m, int n, int k,
-                                       GemmOpt<T> o = GemmOpt<T>()) {
+                                       GemmOpt<T> o = GemmOpt<T>(), int pa = -1, int pb = -1) {
     if constexpr (EMU) {
         if (sm.native & Cat) tile_gemm<T, TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.stage64, o);
-        else ozt::oz_gemm_tc<TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.oz, o);
+        else ozt::oz_gemm_tc<TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.oz, o,
+                                     pa >= 0 ? &sm.pre[pa] : nullptr, pb >= 0 ? &sm.pre[pb] : nullptr);
     } else {
         tile_gemm<T, TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.stage, o);
     }
@@ -624,9 +635,11 @@ __device__ void right_stack_t(const ChainDesc& d, TSmem<T>& sm, int s, double* l
                 __syncthreads();
             } else if (l == lo) {
                 // B(p, j) = U[p][j] = uc[j n + p] (column-major slot)
-                gemm_t<T, EMU, LQMC_FP64E_NATIVE_STACK, false, true>(sm, zb, n, ek, n, slot_U(sm, prev, nn), n, n, n, n, o);
+                gemm_t<T, EMU, LQMC_FP64E_NATIVE_STACK, false, true>(sm, zb, n, ek, n, slot_U(sm, prev, nn), n, n, n, n, o,
+                                                                     kPreK);
             } else {
-                gemm_t<T, EMU, LQMC_FP64E_NATIVE_STACK, false, false>(sm, zb, n, ek, n, za, n, n, n, n, o);   // e^V e^{-dtau K} Z
+                // e^V e^{-dtau K} Z
+                gemm_t<T, EMU, LQMC_FP64E_NATIVE_STACK, false, false>(sm, zb, n, ek, n, za, n, n, n, n, o, kPreK);
             }
             T* t = za; za = zb; zb = t;
         }
@@ -667,7 +680,8 @@ __device__ void left_step_t(const ChainDesc& d, TSmem<T>& sm, int s, int p_in, b
                 for (int j = lane; j < n; j += 32)
                     za[(size_t)i * n + j] = sm.ev_t[i] * za[(size_t)i * n + j];
         }
-        gemm_t<T, EMU, LQMC_FP64E_NATIVE_STACK, true, false>(sm, zb, n, ek, n, za, n, n, n, n);   // e^{-dtau K}^T (e^V Z)
+        // e^{-dtau K}^T (e^V Z)
+        gemm_t<T, EMU, LQMC_FP64E_NATIVE_STACK, true, false>(sm, zb, n, ek, n, za, n, n, n, n, GemmOpt<T>(), kPreKT);
         T* t = za; za = zb; zb = t;
     }
     const double sg = udt_absorb_t<T, EMU>(d, sm, za, first ? nullptr : slot_d(sm, in, nn),
@@ -687,8 +701,10 @@ __device__ void wrap_t(const ChainDesc& d, TSmem<T>& sm, int l) {
         for (int j = lane_id(); j < n; j += 32) g[(size_t)i * n + j] *= sm.iev_t[i];
     GemmOpt<T> o;
     o.cs = sm.ev_t;
-    gemm_t<T, EMU, LQMC_FP64E_NATIVE_WRAP, false, false>(sm, sm.z0, n, mat_expkinv<T>(d), n, g, n, n, n, n, o);
-    gemm_t<T, EMU, LQMC_FP64E_NATIVE_WRAP, false, false>(sm, g, n, sm.z0, n, mat_expk<T>(d), n, n, n, n);
+    gemm_t<T, EMU, LQMC_FP64E_NATIVE_WRAP, false, false>(sm, sm.z0, n, mat_expkinv<T>(d), n, g, n, n, n, n, o,
+                                                         kPreKinv);
+    gemm_t<T, EMU, LQMC_FP64E_NATIVE_WRAP, false, false>(sm, g, n, sm.z0, n, mat_expk<T>(d), n, n, n, n,
+                                                         GemmOpt<T>(), -1, kPreKB);
 }
 
 // Site updates of slice l with delayed rank-k updates (k = d.delay): the accepted flips of
@@ -914,6 +930,13 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     sm.oz.stage = reinterpret_cast<unsigned char*>(p);
     sm.oz.stages = d.oz_stages;
     sm.native = d.native;
+    if constexpr (EMU) {
+        const size_t pre_off[4] = {lay.pre, lay.pre + lay.pre_a, lay.pre + 2 * lay.pre_a, lay.pre + 3 * lay.pre_a};
+        for (int i = 0; i < 4; ++i) {
+            sm.pre[i].slices = reinterpret_cast<const __nv_bfloat16*>(w + pre_off[i]);
+            sm.pre[i].exps = reinterpret_cast<const int*>(w + lay.pre_e) + i * n;
+        }
+    }
     sm.oz.tc = &tcs;
     sm.stage64 = p;   // the float64 LU staging (float kernel) shares the staging region
     const size_t stage_region = stage_region_bytes(sizeof(T) == 4, EMU, d.oz_stages);
@@ -939,7 +962,23 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     // the partner CTA's exchange buffers
     sm.peer_gii = cluster.map_shared_rank(sm.gii, (unsigned)(sp ^ 1));
     sm.peer_xv = cluster.map_shared_rank(sm.xv[0], (unsigned)(sp ^ 1));
+    if constexpr (EMU) {
+        // split the constant operands once per launch: CTA 0 e^{-dtau K} as A (straight and
+        // transposed), CTA 1 e^{+dtau K} as A and e^{-dtau K} as B; the cluster barrier below
+        // publishes them to the other CTA
+        int* scratch = reinterpret_cast<int*>(sm.oz.stage);
+        auto pre_slices = [&](int i) { return const_cast<__nv_bfloat16*>(sm.pre[i].slices); };
+        auto pre_exps = [&](int i) { return const_cast<int*>(sm.pre[i].exps); };
+        if (sp == 0) {
+            ozt::presplit(d.expk, n, true, false, n, n, pre_slices(kPreK), pre_exps(kPreK), scratch);
+            ozt::presplit(d.expk, n, true, true, n, n, pre_slices(kPreKT), pre_exps(kPreKT), scratch);
+        } else {
+            ozt::presplit(d.expkinv, n, true, false, n, n, pre_slices(kPreKinv), pre_exps(kPreKinv), scratch);
+            ozt::presplit(d.expk, n, false, false, n, n, pre_slices(kPreKB), pre_exps(kPreKB), scratch);
+        }
+    }
     cluster.sync();   // both CTAs set up before any remote write
+    if constexpr (EMU) asm volatile("fence.proxy.async;\n" ::: "memory");   // the partner's splits
 
     double max_resid = 0.0, logdet = 0.0, sgn = 1.0;
     uint64_t sweep_id = (uint64_t)d.diag[7];

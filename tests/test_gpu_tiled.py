@@ -191,3 +191,20 @@ def test_fp64e_stalled_tensor_core_wait_reports_timeout():
     assert not good.status().any()
     assert np.isfinite(good.green(0)).all()
     good.close()
+
+
+def test_fp64e_with_every_category_native_is_the_fp64_engine():
+    """Routing every product category of the fp64e engine to native float64 reproduces the
+    plain float64 tiled engine bit for bit (same kernel code, only the GEMMs differ)."""
+    K, field, rng = _setup(10, 4.0, 40, 31)
+    spec = ChainSpec(K, 4.0, 4.0, 40, field)
+    u = rng.random(100 * 40)
+    a = Engine([spec], mode="dqmc", precision="fp64", engine="tiled", rng="replay", stab_every=5)
+    b = Engine([spec], mode="dqmc", precision="fp64e", rng="replay", stab_every=5,
+               fp64e_native=("wrap", "stack", "udt", "green", "update"))
+    for e in (a, b):
+        e.set_uniforms(0, u)
+        e.sweep(1)
+    assert np.array_equal(a.green(0), b.green(0))
+    a.close()
+    b.close()
