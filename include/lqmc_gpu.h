@@ -105,13 +105,15 @@ typedef struct lqmc_params {
     int32_t reserved[4];
 } lqmc_params;
 
-/* product categories of the fp64e engine (lqmc_params.fp64e_native); the LU of the stabilised
- * inverse is always native float64 */
+/* product categories of the fp64e engine (lqmc_params.fp64e_native) */
 #define LQMC_FP64E_NATIVE_WRAP 1     /* the two products of every slice wrap                  */
 #define LQMC_FP64E_NATIVE_STACK 2    /* B-chain products of the UDT stacks                    */
 #define LQMC_FP64E_NATIVE_UDT 4      /* blocked QR updates, Q and T of the UDT factors        */
 #define LQMC_FP64E_NATIVE_GREEN 8    /* U_R^T U_L, T_R T_L^T and U_L Z of the stable inverse   */
 #define LQMC_FP64E_NATIVE_UPDATE 16  /* delayed rank-k updates G -= X Y^T                     */
+#define LQMC_FP64E_NATIVE_LU 32      /* trailing updates of the stabilised inverse's LU (the
+                                        Python Engine's default; emulated, they are equilibrated
+                                        along k and leave a larger stabilisation residual)    */
 
 /* debug bits (lqmc_params.debug), for testing the failure paths */
 #define LQMC_DEBUG_STALL_TC_WAIT 1  /* emulated-GEMM kernel: the first tensor-core step issues

@@ -35,6 +35,7 @@ struct GemmOpt {
     const T* rs = nullptr;        // multiply row i of the product by rs[i]
     const T* cs = nullptr;        // multiply column j of the product by cs[j]
     bool subtract = false;        // C -= product (else C = product)
+    bool kscale = false;          // emulated GEMM: equilibrate along k (ignored by tile_gemm)
 };
 
 // A(i, p) = TA ? a[p * lda + i] : a[i * lda + p];  B(p, j) = TB ? b[j * ldb + p] : b[p * ldb + j]

@@ -152,14 +152,21 @@ __device__ __forceinline__ bool bar_wait(unsigned long long* bar, uint32_t parit
 
 // ---- splitting ---------------------------------------------------------------------------
 
-// N = round(v 2^(55 - e)) for |v| < 2^e (ties away from zero), 0 for zero / non-finite
-__device__ __forceinline__ long long fixed55(double v, int e) {
+// biased exponent of v scaled by 2^off (0 for zero / subnormal, 0x7FF for NaN / Inf)
+__device__ __forceinline__ int biased_exp(double v, int off) {
+    const int be = (int)((__double_as_longlong(v) >> 52) & 0x7FF);
+    return (be == 0 || be == 0x7FF) ? be : be + off;
+}
+
+// N = round(v 2^off 2^(55 - e)) for |v 2^off| < 2^e (ties away from zero), 0 for zero /
+// non-finite
+__device__ __forceinline__ long long fixed55(double v, int e, int off) {
     const long long bits = __double_as_longlong(v);
     const int be = (int)((bits >> 52) & 0x7FF);
     if (be == 0 || be == 0x7FF || e == kNonFinite) return 0;
     const unsigned long long mant = ((unsigned long long)bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
     // v 2^(55 - e) = mant 2^(be - 1075 + 55 - e); |v| < 2^e bounds the left shift by 2
-    const int rs = 1075 - 55 + e - be;
+    const int rs = 1075 - 55 + e - (be + off);
     unsigned long long mag;
     if (rs <= 0) mag = mant << (-rs);
     else mag = (rs < 64) ? ((mant >> (rs - 1)) + 1ull) >> 1 : 0ull;
@@ -174,9 +181,10 @@ __device__ __forceinline__ long long fixed55(double v, int e) {
 // Both passes read 8 consecutive elements of memory per unit with independent loads, so
 // many L2 requests are in flight: the row maxima of the biased exponents are gathered with
 // shared-memory atomics (an exponent of 0x7FF, NaN or Inf, dominates and marks the row).
+// kshift (optional, k ints): element (r, q) is split as X(r, q) 2^kshift[q] (exact).
 template <int BLK>
 __device__ void split_tiles(const double* x, int ld, bool trans, int rows, int k, int* exps,
-                            __nv_bfloat16* dst, int* scratch) {
+                            __nv_bfloat16* dst, int* scratch, const int* kshift = nullptr) {
     const int kp = kpad(k), S = kp / kBK, rp = rows_pad(rows, BLK);
     for (int r = threadIdx.x; r < rows; r += kNT) scratch[r] = 0;
     __syncthreads();
@@ -189,7 +197,7 @@ __device__ void split_tiles(const double* x, int ld, bool trans, int rows, int k
 #pragma unroll
             for (int c = 0; c < 8; ++c)
                 if (q0 + c < k)
-                    emax = max(emax, (int)((__double_as_longlong(x[(size_t)r * ld + q0 + c]) >> 52) & 0x7FF));
+                    emax = max(emax, biased_exp(x[(size_t)r * ld + q0 + c], kshift ? kshift[q0 + c] : 0));
             atomicMax(&scratch[r], emax);
         }
     } else {
@@ -197,11 +205,10 @@ __device__ void split_tiles(const double* x, int ld, bool trans, int rows, int k
         const int g8 = (rows + 7) / 8;
         for (int u = threadIdx.x; u < k * g8; u += kNT) {
             const int q = u / g8, r0 = (u % g8) * 8;
+            const int off = kshift ? kshift[q] : 0;
 #pragma unroll
             for (int c = 0; c < 8; ++c)
-                if (r0 + c < rows)
-                    atomicMax(&scratch[r0 + c],
-                              (int)((__double_as_longlong(x[(size_t)q * ld + r0 + c]) >> 52) & 0x7FF));
+                if (r0 + c < rows) atomicMax(&scratch[r0 + c], biased_exp(x[(size_t)q * ld + r0 + c], off));
         }
     }
     __syncthreads();
@@ -226,7 +233,8 @@ __device__ void split_tiles(const double* x, int ld, bool trans, int rows, int k
             const int q = q0 + c;
             double v = 0.0;
             if (r < rows && q < k) v = trans ? x[(size_t)q * ld + r] : x[(size_t)r * ld + q];
-            const unsigned long long mb = (unsigned long long)(fixed55(v, e) + kBias);
+            const int off = (kshift && q < k) ? kshift[q] : 0;
+            const unsigned long long mb = (unsigned long long)(fixed55(v, e, off) + kBias);
             flo[c] = (uint32_t)(mb & ((1ull << 28) - 1));   // fields of digits 7 .. 4
             fhi[c] = (uint32_t)(mb >> 28);                  // fields of digits 3 .. 0
         }
@@ -250,6 +258,42 @@ __device__ void split_tiles(const double* x, int ld, bool trans, int rows, int k
             *reinterpret_cast<uint4*>(base + (size_t)t * (BLK * kBK)) = make_uint4(w[0], w[1], w[2], w[3]);
         }
     }
+}
+
+// Scratch offsets (ints) of the k-scaling shifts, after the exponent maxima of split_tiles.
+constexpr int kMaxKscale = 1024;
+constexpr int kScratchKA = 2048, kScratchKB = kScratchKA + kMaxKscale;
+
+// out[q] = largest biased exponent (zero and non-finite entries excluded) of X(:, q),
+// X(r, q) = trans ? x[q ld + r] : x[r ld + q], r < rows, q < k
+__device__ inline void k_exponent_max(const double* x, int ld, bool trans, int rows, int k, int* out) {
+    for (int q = threadIdx.x; q < k; q += kNT) out[q] = 0;
+    __syncthreads();
+    if (trans) {
+        const int lane = lane_id();
+        for (int q = warp_id(); q < k; q += kNW) {
+            int emax = 0;
+            for (int r = lane; r < rows; r += 32) {
+                const int be = biased_exp(x[(size_t)q * ld + r], 0);
+                if (be != 0x7FF) emax = max(emax, be);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) emax = max(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+            if (lane == 0) out[q] = emax;
+        }
+    } else {
+        const int g8 = (k + 7) / 8;
+        for (int u = threadIdx.x; u < rows * g8; u += kNT) {
+            const int r = u / g8, q0 = (u % g8) * 8;
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                if (q0 + c < k) {
+                    const int be = biased_exp(x[(size_t)r * ld + q0 + c], 0);
+                    if (be != 0x7FF && be != 0) atomicMax(&out[q0 + c], be);
+                }
+        }
+    }
+    __syncthreads();
 }
 
 // Split a constant operand once: as A (TA: A(i, p) = a[p lda + i]) when as_a, else as B
@@ -371,8 +415,31 @@ __device__ void oz_gemm_tc(double* c, int ldc, const double* a, int lda, const d
     const int* eb = pb ? pb->exps : ws.eb;
     const long long t0 = clock64();
     int* scratch = reinterpret_cast<int*>(ws.stage);   // the stage is idle while splitting
-    if (!pa) split_tiles<kBM>(a, lda, TA, m, k, ws.ea, ws.slices, scratch);
-    if (!pb) split_tiles<kBN>(b, ldb, !TB, n, k, ws.eb, ws.slices + (size_t)kSlices * rows_pad(m, kBM) * kp, scratch);
+    const int* ksa = nullptr;
+    const int* ksb = nullptr;
+    if (opt.kscale && !pa && !pb && k <= kMaxKscale) {
+        // equilibrate along k: A(:, p) 2^s_p and B(p, :) 2^-s_p (exact, the product is
+        // unchanged) with s_p bringing column p of A to [1/2, 1), so that a grading of A's
+        // columns mirrored in B's rows costs no relative accuracy
+        int* ca = scratch + kScratchKA;
+        int* cb = scratch + kScratchKB;
+        k_exponent_max(a, lda, TA, m, k, ca);
+        k_exponent_max(b, ldb, !TB, n, k, cb);
+        for (int p = threadIdx.x; p < k; p += kNT) {
+            int sft = 0;
+            if (ca[p] > 0 && ca[p] < 0x7FF) {
+                sft = 1022 - ca[p];
+                if (cb[p] > 0 && (cb[p] - sft >= 0x7FF - 8 || cb[p] - sft <= 8)) sft = 0;
+            }
+            ca[p] = sft;
+            cb[p] = -sft;
+        }
+        __syncthreads();
+        ksa = ca;
+        ksb = cb;
+    }
+    if (!pa) split_tiles<kBM>(a, lda, TA, m, k, ws.ea, ws.slices, scratch, ksa);
+    if (!pb) split_tiles<kBN>(b, ldb, !TB, n, k, ws.eb, ws.slices + (size_t)kSlices * rows_pad(m, kBM) * kp, scratch, ksb);
     // the slices were written through the generic proxy and are read by bulk copies
     asm volatile("fence.proxy.async;\n" ::: "memory");
     __syncthreads();

@@ -351,6 +351,7 @@ __device__ void lu_solve_blocked(TSmem<double>& sm, double* w, double* rhs, int 
         if (rest > 0) {
             GemmOpt<double> o;
             o.subtract = true;
+            o.kscale = true;
             // W22 -= L21 U12 ; R2 -= L21 R1
             gemm_t<double, EMU, 0, false, false>(sm, w + (size_t)(jb + nb) * n + jb + nb, n,
                                               w + (size_t)(jb + nb) * n + jb, n,
@@ -377,6 +378,7 @@ __device__ void lu_solve_blocked(TSmem<double>& sm, double* w, double* rhs, int 
         if (jb > 0) {
             GemmOpt<double> o;
             o.subtract = true;
+            o.kscale = true;
             // R0 -= U01 R1
             gemm_t<double, EMU, 0, false, false>(sm, rhs, n, w + jb, n, rhs + (size_t)jb * n, n, jb, n, nb, o);
         }
@@ -396,13 +398,16 @@ template <>
 __device__ void lu_solve_dispatch<double, false>(TSmem<double>& sm, int n, double* la, double* sw, int* sing) {
     lu_solve_blocked<false>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
 }
-// The emulated kernel keeps the LU's trailing updates in native float64: the stabilised
-// matrix is graded in its rows and columns, so L21 and U12 can carry opposite grading along
-// the contraction index, where an emulated product (accurate relative to the row / column
-// maxima of its operands) would lose the small terms' relative accuracy.
+// The stabilised matrix is graded in its rows and columns, so L21 and U12 (and U01, R1 of the
+// back substitution) carry mirrored grading along the contraction index; the emulated
+// products of the LU are therefore equilibrated along k (GemmOpt::kscale), which keeps their
+// accuracy relative to each row / column.  LQMC_FP64E_NATIVE_LU keeps them in float64.
 template <>
 __device__ void lu_solve_dispatch<double, true>(TSmem<double>& sm, int n, double* la, double* sw, int* sing) {
-    lu_solve_blocked<false>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
+    if (sm.native & LQMC_FP64E_NATIVE_LU)
+        lu_solve_blocked<false>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
+    else
+        lu_solve_blocked<true>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
 }
 template <>
 __device__ void lu_solve_dispatch<float, false>(TSmem<float>& sm, int n, double* la, double* sw, int* sing) {
