@@ -85,8 +85,9 @@ extern "C" {
  *   refreshes, [12] measurements; tiled kernel only, cycles inside those phases spent in
  *   [13] Householder QR, [14] forming Q and T of the UDT factors, [15] LU solves,
  *   [16] splitting operands of emulated float64 GEMMs, [17] their tensor-core loops
- *   (including [18]), [18] their epilogues (reading and combining the accumulators).
- *   [19..23] reserved.                                                                        */
+ *   (including [18]), [18] their epilogues (reading and combining the accumulators),
+ *   [19] the delayed-update flushes G -= X Y^T, [20] waiting at the per-site cluster barrier.
+ *   [21..23] reserved.                                                                        */
 #define LQMC_DIAG_LEN 24
 
 typedef struct lqmc_params {

@@ -16,9 +16,10 @@ namespace lqmc {
 size_t sweep_fp64_smem_bytes(int n, int flags);
 cudaError_t launch_sweep_fp64(const ChainDesc* d_descs, int n_chains, size_t smem, int n_sweeps,
                               int measure, cudaStream_t stream);
-size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu, int stages);
+size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu, int stages, bool xy_global);
+int sweep_tiled_delay_target(bool fp32, int requested, bool emu);
 int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap, bool emu, int stages);
-size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32, bool emu);
+size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32, bool emu, int xy_delay);
 cudaError_t launch_sweep_tiled(const ChainDesc* d_descs, int n_chains, size_t smem, int precision,
                                int n_sweeps, int measure, cudaStream_t stream);
 }  // namespace lqmc
@@ -266,12 +267,22 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
         } else {
             const bool f32 = kind[c] == kTiledFp32, emu = kind[c] == kTiledFp64e;
             d.flags = 0;
-            // two tensor-core stage buffers unless they would cost delayed-update depth
+            // the delayed-update buffers in shared memory when the target depth fits there,
+            // else in global memory; two tensor-core stage buffers unless they would cost depth
+            const int target = lqmc::sweep_tiled_delay_target(f32, h->p.delay, emu);
             d.oz_stages = 1;
             d.delay = lqmc::sweep_tiled_delay(n, f32, h->p.delay, smem_cap, emu, 1);
-            if (emu && lqmc::sweep_tiled_delay(n, f32, h->p.delay, smem_cap, emu, 2) >= d.delay) d.oz_stages = 2;
-            smem[c] = lqmc::sweep_tiled_smem_bytes(n, f32, d.delay, emu, d.oz_stages);
-            work = (lqmc::sweep_tiled_work_bytes(n, d.n_chunks, f32, emu) + 7) / 8;
+            bool xy_global = false;
+            if (d.delay < target) {
+                xy_global = true;
+                d.delay = target;
+                d.flags |= lqmc::kUpdatesInGlobal;
+                if (emu && lqmc::sweep_tiled_smem_bytes(n, f32, d.delay, emu, 2, true) <= smem_cap) d.oz_stages = 2;
+            } else if (emu && lqmc::sweep_tiled_delay(n, f32, h->p.delay, smem_cap, emu, 2) >= d.delay) {
+                d.oz_stages = 2;
+            }
+            smem[c] = lqmc::sweep_tiled_smem_bytes(n, f32, d.delay, emu, d.oz_stages, xy_global);
+            work = (lqmc::sweep_tiled_work_bytes(n, d.n_chunks, f32, emu, xy_global ? d.delay : 0) + 7) / 8;
             if (smem[c] > smem_cap) { release(h); return fail(h, LQMC_ERR_UNSUPPORTED, "lattice too large for shared memory"); }
         }
         const size_t fcopy = (kind[c] == kTiledFp32) ? 2 * round_up((nn + 1) / 2, kAlign) : 0;

@@ -8,6 +8,7 @@ namespace lqmc {
 enum : int32_t {
     kGreenInGlobal = 1,    // G_up/G_dn live in desc.work instead of shared memory
     kScratchInGlobal = 2,  // the two n x n scratch buffers live in desc.work
+    kUpdatesInGlobal = 4,  // tiled kernel: the delayed-update buffers X, Y live in desc.work
 };
 
 struct ChainDesc {

@@ -518,6 +518,8 @@ __device__ void oz_gemm_tc(double* c, int ldc, const double* a, int lda, const d
             double* ts = reinterpret_cast<double*>(ws.stage);   // [kBM][kTs]
             constexpr int kTs = 33;
             const int ei = (i0 + row < m) ? ea[i0 + row] : 0;
+            // |D_d| <= 8 k 64^2 < 2^22 for the k of this chunk
+            const bool magic_ok = steps * kBK * 8 * 64 * 64 < (1 << 22);
 #pragma unroll 1
             for (int h = 0; h < 2; ++h) {
 #pragma unroll 1
@@ -536,9 +538,17 @@ __device__ void oz_gemm_tc(double* c, int ldc, const double* a, int lda, const d
                     for (int x = 0; x < 8; ++x) {
                         // T = sum_d D_d 2^(7 (7 - d)) / 2^12 from two Horner halves (|D_d| <= 2^24,
                         // each half < 2^46); the 12 dropped low bits are 2^-60 of the largest sum
+                        // the exact FP32 integers to int32: below 2^22 (k <= 127) by the 1.5 2^23
+                        // magic number on the FMA / ALU pipes, else by F2I on the XU pipe
                         int q[kSlices];
+                        if (magic_ok) {
 #pragma unroll
-                        for (int d = 0; d < kSlices; ++d) q[d] = __float2int_rn(__uint_as_float(r[d][x]));
+                            for (int d = 0; d < kSlices; ++d)
+                                q[d] = __float_as_int(__uint_as_float(r[d][x]) + 12582912.0f) - 0x4B400000;
+                        } else {
+#pragma unroll
+                            for (int d = 0; d < kSlices; ++d) q[d] = __float2int_rn(__uint_as_float(r[d][x]));
+                        }
                         long long hi = q[0], lo = q[kSlices / 2];
 #pragma unroll
                         for (int d = 1; d < kSlices / 2; ++d) {

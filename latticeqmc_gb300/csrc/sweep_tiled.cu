@@ -38,8 +38,9 @@ __host__ __device__ constexpr size_t align256(size_t b) { return (b + 255) / 256
 // the UDT slots of both spins.
 template <typename T>
 struct TiledLayout {
-    size_t nn, g, z, s, oz, oz_ea, spin_block, slot, total, g_slots, pre, pre_a, pre_b, pre_e;
-    __host__ __device__ TiledLayout(int n, int n_chunks, bool emu = false) {
+    size_t nn, g, z, s, oz, oz_ea, xy, spin_block, slot, total, g_slots, pre, pre_a, pre_b, pre_e;
+    // xy_delay > 0: the spin blocks also hold the delayed-update buffers X, Y (n x (k + 1))
+    __host__ __device__ TiledLayout(int n, int n_chunks, bool emu = false, int xy_delay = 0) {
         nn = (size_t)n * n;
         g = 0;                                              // G of the spin       (T)
         z = g + align256(nn * sizeof(T));                   // Z0, Z1 GEMM temps   (T)
@@ -48,7 +49,8 @@ struct TiledLayout {
         // the largest product of the kernel has m, n, k <= n_sites
         const size_t oz_bytes = emu ? align256(ozt::slice_elems(n, n, n) * 2) : 0;
         oz_ea = oz + oz_bytes;                              // emulated GEMM exponents (int)
-        spin_block = oz_ea + (emu ? align256(2 * (size_t)n * sizeof(int)) : 0);
+        xy = oz_ea + (emu ? align256(2 * (size_t)n * sizeof(int)) : 0);
+        spin_block = xy + (xy_delay > 0 ? align256(2 * (size_t)n * (xy_delay + 1) * sizeof(T)) : 0);
         g_slots = 2 * spin_block;
         slot = align256(2 * nn * sizeof(T) + (size_t)(n + 1) * sizeof(double));
         pre = g_slots + (size_t)(2 * n_chunks + 4) * slot;
@@ -88,8 +90,10 @@ struct TSmem {
     T* stage;
     T* dx;        // delayed updates: X (n x (kd + 1)), G_eff = G - X Y^T
     T* dy;        // Y (n x (kd + 1))
-    double* gii;  // [2 parity][2 spins] diagonal of G_eff for the current site, both spins
-    long long* sub;   // [3] clock cycles: Householder QR, Q and T formation, LU solve
+    double* gii;  // by site parity p = i & 1: [2 p + spin] ratio factors R_sigma of both
+                  // spins, [4 + p] this spin's update coefficient D / R, [6 + p] the uniform
+    long long* sub;   // clock cycles (thread 0): [0] Householder QR, [1] Q and T formation,
+                      // [2] LU solve, [3..5] emulated GEMMs, [6] update flushes, [7] site barrier
     ozt::Workspace oz;    // emulated float64 GEMM: slice buffers, exponents, staging, TMEM state
     double* panel;    // blocked LU panel, n x (panel_width + 1); overlays stage, dx, dy
     int* piv;         // [kPanel] panel pivots
@@ -739,6 +743,8 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int sw, 
         const int8_t s_il = f[i];
         const int par = 2 * (i & 1);
         if (warp_id() == 0) {
+            // this spin's factor R_sigma = 1 + D_sigma (1 - G_eff,ii), its update coefficient
+            // D_sigma / R_sigma and the site's uniform, once per CTA; the factors are exchanged
             const int lane = lane_id();
             T part = T(0);
             for (int q = lane; q < m; q += 32) part = fma(sm.dx[(size_t)i * ld + q], sm.dy[(size_t)i * ld + q], part);
@@ -746,25 +752,27 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int sw, 
             for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
             if (lane == 0) {
                 const double gv = (double)(g[(size_t)i * n + i] - part);
-                sm.gii[par + sp] = gv;
-                sm.peer_gii[par + sp] = gv;
+                const double ep = s_il > 0 ? d.c[0] : d.c[1];
+                const double em = s_il > 0 ? d.c[1] : d.c[0];
+                const double dl = (sp ? em : ep) - 1.0;
+                const double r = 1.0 + dl * (1.0 - gv);
+                sm.gii[par + sp] = r;
+                sm.peer_gii[par + sp] = r;
+                sm.gii[4 + (i & 1)] = dl / r;
+                const int pos = step * n + i;
+                sm.gii[6 + (i & 1)] = (d.rng == LQMC_RNG_REPLAY)
+                                          ? d.uniforms[(size_t)sw * n * L + pos]
+                                          : philox_uniform(d.seed, (uint64_t)d.chain_id, sweep_id, (uint64_t)pos);
             }
         }
+        const long long tb = clock64();
         cluster.sync();
-        const int pos = step * n + i;
-        double u;
-        if (d.rng == LQMC_RNG_REPLAY) u = d.uniforms[(size_t)sw * n * L + pos];
-        else u = philox_uniform(d.seed, (uint64_t)d.chain_id, sweep_id, (uint64_t)pos);
-        const double gi0 = sm.gii[par], gi1 = sm.gii[par + 1];
-        const double ep = s_il > 0 ? d.c[0] : d.c[1];
-        const double em = s_il > 0 ? d.c[1] : d.c[0];
-        const double dl_up = ep - 1.0, dl_dn = em - 1.0;
-        const double r_up = 1.0 + dl_up * (1.0 - gi0), r_dn = 1.0 + dl_dn * (1.0 - gi1);
-        const double ratio = r_up * r_dn;
-        const bool acc = (u <= ratio);
+        if (threadIdx.x == 0) sm.sub[7] += clock64() - tb;
+        const double ratio = sm.gii[par] * sm.gii[par + 1];   // R_up R_dn, the same product in both CTAs
+        const bool acc = (sm.gii[6 + (i & 1)] <= ratio);
         if (sp == 0 && d.record && threadIdx.x == 0) d.decisions[((size_t)sw * L + step) * n + i] = acc ? 1 : 0;
         if (!acc) continue;
-        const T a = sp ? (T)(dl_dn / r_dn) : (T)(dl_up / r_up);
+        const T a = (T)sm.gii[4 + (i & 1)];
 #pragma unroll
         for (int q = 0; q < kPer; ++q) {
             const int j = threadIdx.x + q * kNT;
@@ -783,16 +791,20 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int sw, 
         }
         __syncthreads();
         if (++m == kd) {
+            const long long tf = clock64();
             GemmOpt<T> o;
             o.subtract = true;
             gemm_t<T, EMU, LQMC_FP64E_NATIVE_UPDATE, false, true>(sm, g, n, sm.dx, ld, sm.dy, ld, n, n, m, o);
+            if (threadIdx.x == 0) sm.sub[6] += clock64() - tf;
             m = 0;
         }
     }
     if (m > 0) {
+        const long long tf = clock64();
         GemmOpt<T> o;
         o.subtract = true;
         gemm_t<T, EMU, LQMC_FP64E_NATIVE_UPDATE, false, true>(sm, g, n, sm.dx, ld, sm.dy, ld, n, n, m, o);
+        if (threadIdx.x == 0) sm.sub[6] += clock64() - tf;
     }
     __syncthreads();
 }
@@ -877,7 +889,7 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     __shared__ ChainDesc d;
     __shared__ int accepted;
     __shared__ int singular;
-    __shared__ long long sub[6];
+    __shared__ long long sub[8];
     __shared__ ozt::Tc tcs;
     __shared__ double peer_resid;
     const int sp = (int)cluster.block_rank();   // spin of this CTA
@@ -885,7 +897,7 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
         d = descs[blockIdx.x >> 1];
         accepted = 0;
         singular = 0;
-        for (int k = 0; k < 6; ++k) sub[k] = 0;
+        for (int k = 0; k < 8; ++k) sub[k] = 0;
         peer_resid = 0.0;
     }
     __syncthreads();
@@ -895,7 +907,8 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     }
     const int n = d.n;
     const size_t nn = (size_t)n * n;
-    TiledLayout<T> lay(n, d.n_chunks, EMU);
+    const bool xy_global = (d.flags & kUpdatesInGlobal) != 0;
+    TiledLayout<T> lay(n, d.n_chunks, EMU, xy_global ? d.delay : 0);
     unsigned char* w = reinterpret_cast<unsigned char*>(d.work);
     unsigned char* wb = w + (size_t)sp * lay.spin_block;   // this spin's block
     TSmem<T> sm;
@@ -929,7 +942,7 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     sm.yt[1] = tp; tp += n;
     p = reinterpret_cast<double*>(tp);
     p = smem + (((p - smem) + 3) & ~(ptrdiff_t)3);
-    sm.gii = p; p += 4;
+    sm.gii = p; p += 8;
     if (EMU) p = smem + (((p - smem) + 15) & ~(ptrdiff_t)15);   // 128-byte aligned stage
     sm.stage = reinterpret_cast<T*>(p);
     sm.oz.stage = reinterpret_cast<unsigned char*>(p);
@@ -951,14 +964,19 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     sm.oz.eb = sm.oz.ea + n;
     sm.oz.cycles = sub + 3;   // splitting, product loops, epilogues
     const size_t dsz = (size_t)n * (d.delay + 1);
-    sm.dx = tp; tp += dsz;
-    sm.dy = tp; tp += dsz;
+    if (xy_global) {
+        sm.dx = reinterpret_cast<T*>(wb + lay.xy);
+        sm.dy = sm.dx + dsz;
+    } else {
+        sm.dx = tp; tp += dsz;
+        sm.dy = tp; tp += dsz;
+    }
     {
         // The LU panel overlays the GEMM staging and the delayed-update buffers: the panel is
         // live only between a panel load and the trailing-update GEMMs, and X / Y only
         // between refreshes.  The pivot list follows the larger of the two.
         sm.panel = p;
-        const size_t rbytes = stage_region + 2 * dsz * sizeof(T);
+        const size_t rbytes = stage_region + (xy_global ? 0 : 2 * dsz * sizeof(T));
         const size_t pbytes = (size_t)n * (panel_width(n) + 1) * sizeof(double);
         unsigned char* q = reinterpret_cast<unsigned char*>(p) + (rbytes > pbytes ? rbytes : pbytes);
         q = reinterpret_cast<unsigned char*>(((uintptr_t)q + 15) & ~(uintptr_t)15);
@@ -1045,7 +1063,7 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
             d.diag[2] = max_resid;
             d.diag[7] += (double)n_sweeps;
             for (int k = 0; k < 5; ++k) d.diag[8 + k] = (double)ph[k];
-            for (int k = 0; k < 6; ++k) d.diag[13 + k] = (double)sub[k];
+            for (int k = 0; k < 8; ++k) d.diag[13 + k] = (double)sub[k];
             if (max_resid > d.drift_tol) atomicOr(d.status, LQMC_STATUS_DRIFT);
         }
     }
@@ -1056,14 +1074,14 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
 }
 
 // bytes of dynamic shared memory / per-chain global work of the tiled kernel
-size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu, int stages) {
+size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu, int stages, bool xy_global) {
     size_t v = (size_t)(kNW + 8 + 9 * n);
     v = (v + 3) & ~(size_t)3;                                   // doubles
     const size_t ts = fp32 ? 4 : 8;
     const size_t tvec = 6 * (size_t)n * ts;                     // T vectors, bytes
     v += ((tvec + 7) / 8 + 3) & ~(size_t)3;
-    v += 4;                                                     // gii
-    const size_t rbytes = stage_region_bytes(fp32, emu, stages) + 2 * (size_t)n * (delay + 1) * ts;
+    v += 8;                                                     // gii
+    const size_t rbytes = stage_region_bytes(fp32, emu, stages) + (xy_global ? 0 : 2 * (size_t)n * (delay + 1) * ts);
     const size_t pbytes = (size_t)n * (panel_width(n) + 1) * sizeof(double);
     size_t total = v * sizeof(double) + (rbytes > pbytes ? rbytes : pbytes) + 16 + kPanel * sizeof(int);
     if (emu) {
@@ -1073,15 +1091,21 @@ size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu, int stages)
     return total;
 }
 
-// largest delayed-update depth <= requested (0: 32 in fp32, 16 in fp64) that fits `cap`
+// delayed-update depth wanted: requested, or 32 in fp32, 24 with emulated GEMMs, 16 in fp64
+int sweep_tiled_delay_target(bool fp32, int requested, bool emu) {
+    return requested > 0 ? requested : (fp32 ? 32 : (emu ? 24 : 16));
+}
+
+// largest delayed-update depth <= the target whose buffers fit `cap` in shared memory
 int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap, bool emu, int stages) {
-    int k = requested > 0 ? requested : (fp32 ? 32 : 16);
-    while (k > 1 && sweep_tiled_smem_bytes(n, fp32, k, emu, stages) > cap) --k;
+    int k = sweep_tiled_delay_target(fp32, requested, emu);
+    while (k > 1 && sweep_tiled_smem_bytes(n, fp32, k, emu, stages, false) > cap) --k;
     return k;
 }
 
-size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32, bool emu) {
-    return fp32 ? TiledLayout<float>(n, n_chunks).total : TiledLayout<double>(n, n_chunks, emu).total;
+size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32, bool emu, int xy_delay) {
+    return fp32 ? TiledLayout<float>(n, n_chunks, false, xy_delay).total
+                : TiledLayout<double>(n, n_chunks, emu, xy_delay).total;
 }
 
 template <typename T, bool EMU>

@@ -216,7 +216,8 @@ class Engine:
                 "phase_cycles": {"recompute": d[8], "update": d[9], "wrap": d[10],
                                  "stabilise": d[11], "measure": d[12]},
                 "sub_cycles": {"qr": d[13], "q_and_t": d[14], "lu": d[15],
-                               "oz_split": d[16], "oz_mma": d[17], "oz_epilogue": d[18]}}
+                               "oz_split": d[16], "oz_mma": d[17], "oz_epilogue": d[18],
+                               "flush": d[19], "site_barrier": d[20]}}
 
     def status(self):
         s = np.empty(len(self.chains), dtype=np.int32)

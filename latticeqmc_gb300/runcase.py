@@ -26,6 +26,7 @@ def main():
     ap.add_argument("--chains", type=int, default=1)
     ap.add_argument("--sweeps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=0)
+    ap.add_argument("--delay", type=int, default=0, help="delayed-update depth (0: automatic)")
     a = ap.parse_args()
     m = HubbardModel(u=a.u, t=1, mu=0)
     m.build_square(a.side)
@@ -35,7 +36,7 @@ def main():
     specs = [ChainSpec(K, a.u, a.beta, a.L, (2 * rng.integers(0, 2, (n, a.L)) - 1).astype(np.int8))
              for _ in range(a.chains)]
     eng = Engine(specs, mode="dqmc", precision=a.precision, rng="philox", seed=1,
-                 stab_every=a.stab, engine=a.engine)
+                 stab_every=a.stab, engine=a.engine, delay=a.delay)
     if a.warmup:
         eng.sweep(a.warmup)
         eng.green(0)
@@ -46,7 +47,7 @@ def main():
     d = eng.diagnostics(0)
     pc = d["phase_cycles"]
     tot = max(sum(pc.values()), 1.0)
-    print(f"{a.side}x{a.side} L={a.L} {a.precision} chains={a.chains}: "
+    print(f"{a.side}x{a.side} L={a.L} {a.precision} chains={a.chains} delay={a.delay or 'auto'}: "
           f"{dt * 1e3 / a.sweeps:.1f} ms/sweep, residual {d['max_residual']:.1e}, "
           + " ".join(f"{k}={100 * v / tot:.1f}%" for k, v in pc.items()) + " | "
           + " ".join(f"{k}={100 * v / tot:.1f}%" for k, v in d["sub_cycles"].items()))

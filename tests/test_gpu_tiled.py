@@ -199,8 +199,9 @@ def test_fp64e_with_every_category_native_is_the_fp64_engine():
     K, field, rng = _setup(10, 4.0, 40, 31)
     spec = ChainSpec(K, 4.0, 4.0, 40, field)
     u = rng.random(100 * 40)
-    a = Engine([spec], mode="dqmc", precision="fp64", engine="tiled", rng="replay", stab_every=5)
-    b = Engine([spec], mode="dqmc", precision="fp64e", rng="replay", stab_every=5,
+    a = Engine([spec], mode="dqmc", precision="fp64", engine="tiled", rng="replay", stab_every=5,
+               delay=16)
+    b = Engine([spec], mode="dqmc", precision="fp64e", rng="replay", stab_every=5, delay=16,
                fp64e_native=("wrap", "stack", "udt", "green", "update", "lu"))
     for e in (a, b):
         e.set_uniforms(0, u)
