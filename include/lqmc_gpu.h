@@ -190,6 +190,16 @@ int lqmc_get_decisions(lqmc_handle* h, int32_t chain, int8_t* decisions, size_t 
 /* Per-chain diagnostics, LQMC_DIAG_LEN doubles (layout above). */
 int lqmc_get_diagnostics(lqmc_handle* h, int32_t chain, double* diag);
 
+/* Resume a chain from a checkpoint: restore its diagnostics (LQMC_DIAG_LEN doubles as
+ * lqmc_get_diagnostics returned them; [7] is the sweep counter that keys the Philox stream),
+ * its sum of G ((2, N, N)) and its observable sums (LQMC_OBS_LEN(N); [0] is the measurement
+ * count).  Each pointer may be NULL to keep the current values.  Together with
+ * lqmc_set_field this restores everything the next sweep depends on: G is recomputed from
+ * the field at the start of every sweep.  No reference counterpart (the reference's runs
+ * cannot be resumed); serves the per-chain checkpoint / resume of long beta / U scans. */
+int lqmc_set_chain_state(lqmc_handle* h, int32_t chain, const double* diag, const double* green_sum,
+                         const double* obs);
+
 /* Per-chain LQMC_STATUS_* bit masks, n_chains int32 (0 = healthy). */
 int lqmc_get_status(lqmc_handle* h, int32_t* status);
 

@@ -15,11 +15,12 @@ from .engine import ChainSpec, Engine
 from .hubbard import HubbardModel
 from .lattice import Lattice
 from .lqmc import LatticeQMC
+from .scan import scan
 from .tools import (check_params, compute_pole_gf_tau, fermi_fct, filling, local_gf,
                     local_moment, matsubara_frequencies, pole_gf_tau)
 
 __all__ = ["Configuration", "ChainSpec", "Engine", "HubbardModel", "Lattice", "LatticeQMC",
-           "measure", "measure_betas", "check_params", "compute_pole_gf_tau", "fermi_fct",
+           "measure", "measure_betas", "scan", "check_params", "compute_pole_gf_tau", "fermi_fct",
            "filling", "local_gf", "local_moment", "matsubara_frequencies", "pole_gf_tau"]
 
 _DEFAULT_CHAINS = 16

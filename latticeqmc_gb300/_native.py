@@ -65,6 +65,7 @@ _SIGS = [
     ("lqmc_reset_measurements", ctypes.c_int, [_P]),
     ("lqmc_get_decisions", ctypes.c_int, [_P, _I32, _P, ctypes.c_size_t]),
     ("lqmc_get_diagnostics", ctypes.c_int, [_P, _I32, _P]),
+    ("lqmc_set_chain_state", ctypes.c_int, [_P, _I32, _P, _P, _P]),
     ("lqmc_get_status", ctypes.c_int, [_P, _P]),
     ("lqmc_get_launch_count", ctypes.c_int, [_P, _P]),
     ("lqmc_last_error", ctypes.c_char_p, [_P]),

@@ -616,6 +616,26 @@ int lqmc_get_decisions(lqmc_handle* h, int32_t chain, int8_t* decisions, size_t 
     return LQMC_OK;
 }
 
+int lqmc_set_chain_state(lqmc_handle* h, int32_t chain, const double* diag, const double* green_sum,
+                         const double* obs) {
+    int rc = check_chain(h, chain);
+    if (rc) return rc;
+    if ((rc = sync_last(h))) return rc;
+    const ChainDesc& d = h->desc[chain];
+    if (diag) {
+        if (!(diag[7] >= 0.0) || diag[7] != (double)(int64_t)diag[7])
+            return fail(h, LQMC_ERR_INVALID, "diagnostics[7] (sweep counter) must be a non-negative integer");
+        LQMC_CK(h, cudaMemcpy(d.diag, diag, LQMC_DIAG_LEN * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    if (green_sum)
+        LQMC_CK(h, cudaMemcpy(d.gsum, green_sum, 2 * (size_t)d.n * d.n * sizeof(double), cudaMemcpyHostToDevice));
+    if (obs) {
+        if (!(obs[0] >= 0.0)) return fail(h, LQMC_ERR_INVALID, "observables[0] (measurement count) must be >= 0");
+        LQMC_CK(h, cudaMemcpy(d.obs, obs, LQMC_OBS_LEN(d.n) * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    return LQMC_OK;
+}
+
 int lqmc_get_diagnostics(lqmc_handle* h, int32_t chain, double* diag) {
     int rc = check_chain(h, chain);
     if (rc) return rc;

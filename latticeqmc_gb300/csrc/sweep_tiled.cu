@@ -854,28 +854,34 @@ __device__ void measure_t(const ChainDesc& d, TSmem<T>& sm) {
     ep = block_sum(ep, sm.sv);
     dc = block_sum(dc, sm.sv);
     dn = block_sum(dn, sm.sv);
-    if (threadIdx.x == 0) {
-        atomicAdd(&obs[1], ek);
-        if (sp == 0) {
-            obs[0] += 1.0;
-            obs[2] += d.u * ep;
-            obs[3] += dc / n;
-            obs[4] += dn / n;
-        }
-    }
+    // entries both spins add to are added in a fixed order (spin up, cluster barrier, spin
+    // down), so that the sums do not depend on which CTA gets there first
     double* onn = obs + LQMC_OBS_HEADER + 2 * n;
     double* osz = onn + nn;
     const double* ns = sm.xv[sp];
-    for (int i = warp_id(); i < n; i += kNW)
-        for (int j = lane_id(); j < n; j += 32) {
-            const size_t e = (size_t)i * n + j;
-            const double del = (i == j) ? 1.0 : 0.0;
-            const double same = ns[i] * ns[j] + (del - (double)g[(size_t)j * n + i]) * (double)g[e];
-            const double cross = sp == 0 ? nu[i] * nd[j] + nd[i] * nu[j] : 0.0;
-            atomicAdd(&onn[e], same + cross);
-            atomicAdd(&osz[e], 0.25 * (same - cross));
+    for (int turn = 0; turn < 2; ++turn) {
+        if (turn == sp) {
+            if (threadIdx.x == 0) {
+                obs[1] += ek;
+                if (sp == 0) {
+                    obs[0] += 1.0;
+                    obs[2] += d.u * ep;
+                    obs[3] += dc / n;
+                    obs[4] += dn / n;
+                }
+            }
+            for (int i = warp_id(); i < n; i += kNW)
+                for (int j = lane_id(); j < n; j += 32) {
+                    const size_t e = (size_t)i * n + j;
+                    const double del = (i == j) ? 1.0 : 0.0;
+                    const double same = ns[i] * ns[j] + (del - (double)g[(size_t)j * n + i]) * (double)g[e];
+                    const double cross = sp == 0 ? nu[i] * nd[j] + nd[i] * nu[j] : 0.0;
+                    onn[e] += same + cross;
+                    osz[e] += 0.25 * (same - cross);
+                }
         }
-    __syncthreads();
+        cluster.sync();
+    }
 }
 
 }  // namespace

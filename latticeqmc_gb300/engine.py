@@ -219,6 +219,40 @@ class Engine:
                                "oz_split": d[16], "oz_mma": d[17], "oz_epilogue": d[18],
                                "flush": d[19], "site_barrier": d[20]}}
 
+    # -- checkpoint / resume -------------------------------------------------------------
+    def checkpoint(self, path):
+        """Write every chain's state (field, diagnostics with the Philox sweep counter, sum of
+        G, observable sums) and the engine's settings to an .npz file."""
+        arrays = {"n_sites": np.array([c.n for c in self.chains]),
+                  "n_slices": np.array([c.L for c in self.chains]),
+                  "settings": np.array([self.mode, self.precision, self.rng, str(self.stab_every)])}
+        for k in range(len(self.chains)):
+            d = np.empty(_native.DIAG_LEN)
+            self._h.call("lqmc_get_diagnostics", int(k), ptr(d))
+            gsum, _ = self.green_sum(k)
+            arrays[f"field_{k}"] = self.field(k)
+            arrays[f"diag_{k}"] = d
+            arrays[f"gsum_{k}"] = gsum
+            arrays[f"obs_{k}"] = self.observables_raw(k)
+        np.savez(path, **arrays)
+
+    def restore(self, path):
+        """Resume from a checkpoint of an engine with the same chains and settings (the seed
+        is not stored: pass the same seed to the new Engine)."""
+        z = np.load(path)
+        if (list(z["n_sites"]) != [c.n for c in self.chains]
+                or list(z["n_slices"]) != [c.L for c in self.chains]):
+            raise ValueError("checkpoint was written for different chains")
+        want = [self.mode, self.precision, self.rng, str(self.stab_every)]
+        if list(z["settings"]) != want:
+            raise ValueError(f"checkpoint settings {list(z['settings'])} differ from {want}")
+        for k in range(len(self.chains)):
+            self.set_field(k, z[f"field_{k}"])
+            d = np.ascontiguousarray(z[f"diag_{k}"], dtype=np.float64)
+            g = np.ascontiguousarray(z[f"gsum_{k}"], dtype=np.float64)
+            o = np.ascontiguousarray(z[f"obs_{k}"], dtype=np.float64)
+            self._h.call("lqmc_set_chain_state", int(k), ptr(d), ptr(g), ptr(o))
+
     def status(self):
         s = np.empty(len(self.chains), dtype=np.int32)
         self._h.check(self._h.lib.lqmc_get_status(self._h.h, ptr(s)))
