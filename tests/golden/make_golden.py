@@ -224,10 +224,41 @@ def u0_fixture():
     np.savez_compressed(os.path.join(HERE, "u0_known.npz"), **out)
 
 
+def lattice_fixtures():
+    """Kinetic matrices of the reference's other lattice prefabs (lattice.py:364-421), built
+    through HubbardModel with its lattice replaced: hexagonal (two-atom cell) and cubic, open
+    boundaries, and the reference's periodic hexagonal lattices where its distance search
+    finds the wrap-around bonds."""
+    from lqmc.lattice import Lattice as RefLattice
+    out = {}
+    for shape in [(2, 2), (3, 2), (2, 3), (4, 3)]:
+        m = HubbardModel(u=4, t=1, mu=0)
+        m.lattice = RefLattice.hexagonal()
+        m.lattice.build(shape)
+        out["hex_open_%dx%d" % shape] = m.ham_kinetic()
+    for shape in [(2, 2, 2), (3, 2, 2), (3, 3, 2)]:
+        m = HubbardModel(u=4, t=1, mu=0)
+        m.lattice = RefLattice.cubic()
+        m.lattice.build(shape)
+        out["cubic_open_%dx%dx%d" % shape] = m.ham_kinetic()
+    for shape in [(3, 3), (4, 3)]:
+        m = HubbardModel(u=4, t=1, mu=0)
+        m.lattice = RefLattice.hexagonal()
+        m.lattice.build(shape)
+        try:
+            m.lattice.set_periodic_boundary((0, 1))
+            out["hex_pbc_%dx%d" % shape] = m.ham_kinetic()
+        except ValueError:
+            pass
+    np.savez_compressed(os.path.join(HERE, "kinetic_lattices.npz"), **out)
+
+
 def main():
-    which = sys.argv[1:] or ["kinetic", "compat", "det", "run", "u0"]
+    which = sys.argv[1:] or ["kinetic", "lattices", "compat", "det", "run", "u0"]
     if "kinetic" in which:
         kinetic_fixtures()
+    if "lattices" in which:
+        lattice_fixtures()
     if "compat" in which:
         compat_fixture(2, 4.0, 2.0, 20, seed=7, n_sweeps=40)
         compat_fixture(4, 4.0, 4.0, 40, seed=11, n_sweeps=8)

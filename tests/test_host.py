@@ -53,7 +53,11 @@ def test_lattice_errors():
     with pytest.raises(ValueError):
         Lattice.square().set_periodic_boundary(0)
     with pytest.raises(ValueError):
-        Lattice.square((0, 3))
+        Lattice.square(shape=(0, 3))
+    with pytest.raises(ValueError):
+        Lattice.cubic(shape=(2, 2, 2)).set_periodic_boundary(3)
+    with pytest.raises(ValueError):
+        Lattice.square(neighbour_dist=2)
 
 
 def test_configuration_draws_like_reference():
@@ -134,3 +138,38 @@ def test_library_loads_and_exports_every_declared_symbol():
         rc = lib.lqmc_create(ctypes.byref(p), ctypes.byref(h))
         assert rc in (-1, -2)
         assert lib.lqmc_last_error(None)
+
+
+def test_other_lattices_match_reference_kinetic_matrices():
+    """Hexagonal (two-atom cell) and cubic prefabs, open boundaries: K equal to the
+    reference's (tests/golden/kinetic_lattices.npz, recorded by make_golden.py)."""
+    z = golden("kinetic_lattices.npz")
+    for key in z.files:
+        kind, bc, dims = key.split("_")
+        shape = tuple(int(s) for s in dims.split("x"))
+        m = HubbardModel(u=4, t=1, mu=0)
+        m.lattice = Lattice.hexagonal() if kind == "hex" else Lattice.cubic()
+        m.lattice.build(shape)
+        if bc == "pbc":
+            m.lattice.set_periodic_boundary(tuple(range(len(shape))))
+        np.testing.assert_array_equal(m.ham_kinetic(), z[key], err_msg=key)
+
+
+def test_periodic_hexagonal_and_cubic_lattices():
+    """Periodic boundaries by minimal image: honeycomb sites have 3 bonds, all A-B; simple
+    cubic sites have 6 (sizes >= 3; the reference's distance search cannot close these)."""
+    for shape in ((3, 3), (4, 3), (5, 4)):
+        lat = Lattice.hexagonal(shape=shape)
+        lat.set_periodic_boundary((0, 1))
+        for i in range(lat.n_sites):
+            nbs = lat.nearest_neighbours(i)
+            assert len(nbs) == 3
+            assert all(lat.indices[j][-1] != lat.indices[i][-1] for j in nbs)
+    lat = Lattice.cubic(shape=(3, 4, 3))
+    lat.set_periodic_boundary((0, 1, 2))
+    a = lat.adjacency()
+    assert np.array_equal(a, a.T) and set(a.sum(1)) == {6.0}
+    m = HubbardModel(u=4, t=1, mu=0)
+    m.lattice = Lattice.cubic()
+    m.build(3, 3, None)
+    assert m.n_sites == 9
