@@ -53,6 +53,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "site-updates/s (sweeps/s beside it), DQMC sweep of batched Markov chains"
+# DRAM traffic of one fp64e sweep launch of the square16_beta8 workload (64 chains), from ncu
+FP64E_TRAFFIC = 4.106e11
 UNIT = "site-updates/s"
 
 
@@ -468,7 +470,11 @@ def main():
                 tpeak, tsrc = 1700.0, "fallback sustained bf16 figure (of fallback)"
             achieved = 36.0 * fp64_eq
             roof = {"bound": "tensor", "achieved": achieved, "peak": tpeak, "unit": "TFLOP/s",
-                    "frac": achieved / tpeak, "traffic": None, "peak_source": tsrc,
+                    "frac": achieved / tpeak, "peak_source": tsrc,
+                    "traffic": FP64E_TRAFFIC if args.chains == 64 else None,
+                    "traffic_unit": "DRAM bytes per launch (one sweep of all chains)",
+                    "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
+                                      "fp64e sweep kernel on this workload (mean of 2 launches)",
                     "kernel": "sweep kernel of the fp64e engine (BF16 slice products: 36 per "
                               "algorithmic float64 flop)",
                     "fp64_equivalent": {"achieved": fp64_eq, "peak": r["peak"], "unit": "TFLOP/s",

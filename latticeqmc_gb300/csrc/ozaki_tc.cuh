@@ -20,10 +20,12 @@
 // K-major, no-swizzle layout (8 x 16-byte core matrices), grouped so that all eight slices
 // of one (row block, 16-wide k step) are one contiguous block.  One thread then moves a
 // whole k step of A (32 KB) and of B (16 KB) into shared memory with two bulk asynchronous
-// copies completing on an mbarrier, issues the 36 MMAs of the step and commits them to a
-// second mbarrier; with two stage buffers the copies of step s + 1 overlap the MMAs of step
-// s.  The epilogue reads the accumulators with tcgen05.ld (warp w reads TMEM lanes
-// 32 (w mod 4) ..), combines them in int64 and scales by exponent arithmetic.
+// copies completing on an mbarrier, issues the step's MMAs (one per A digit t, N = 64 (8 - t)
+// cut at 256: 12 instructions for the 36 digit pairs) and commits them to a second mbarrier;
+// with two stage buffers the copies of step s + 1 overlap the MMAs of step s.  The epilogue
+// reads the accumulators with tcgen05.ld (warp w reads TMEM lanes 32 (w mod 4) ..), combines
+// them in int64 and converts to float64 with integer operations, the scale folded into the
+// exponent.
 //
 // Every wait is bounded: a wait that runs out sets Tc::fail, after which this and every later
 // call return without issuing work; the kernel reports the flag as a status bit.
