@@ -45,6 +45,9 @@ extern "C" {
 /* algorithm modes */
 #define LQMC_MODE_COMPAT 0   /* replays lqmc.py:301-347 arithmetic, defects included     */
 #define LQMC_MODE_DQMC 1     /* textbook DQMC, QR/UDV stabilised                          */
+#define LQMC_MODE_DET 2      /* the reference's determinant mode (lqmc.py:236-299): every
+                                ratio from det M of the flipped configuration, unstabilised
+                                products; float64, shared-memory kernel, a slow check path */
 
 /* precisions */
 #define LQMC_PREC_FP64 0     /* every floating-point operation in float64                */

@@ -15,7 +15,7 @@ LIB_PATH = os.path.join(_PKG, "liblqmc_gpu.so")
 LQMC_OK = 0
 ERRORS = {-1: "LQMC_ERR_INVALID", -2: "LQMC_ERR_CUDA", -3: "LQMC_ERR_STATE",
           -4: "LQMC_ERR_UNSUPPORTED", -5: "LQMC_ERR_NUMERIC", -6: "LQMC_ERR_NOMEM"}
-MODES = {"compat": 0, "dqmc": 1}
+MODES = {"compat": 0, "dqmc": 1, "det": 2}
 PRECISIONS = {"fp64": 0, "mixed": 1, "fp64e": 2}
 RNGS = {"replay": 0, "philox": 1}
 ENGINES = {"auto": 0, "smem": 1, "tiled": 2}

@@ -142,7 +142,7 @@ int lqmc_abi_version(void) { return LQMC_ABI_VERSION; }
 int lqmc_create(const lqmc_params* params, lqmc_handle** out) {
     if (!params || !out) return fail(nullptr, LQMC_ERR_INVALID, "null argument");
     *out = nullptr;
-    if (params->mode != LQMC_MODE_COMPAT && params->mode != LQMC_MODE_DQMC)
+    if (params->mode != LQMC_MODE_COMPAT && params->mode != LQMC_MODE_DQMC && params->mode != LQMC_MODE_DET)
         return fail(nullptr, LQMC_ERR_INVALID, "unknown mode");
     if (params->precision != LQMC_PREC_FP64 && params->precision != LQMC_PREC_MIXED &&
         params->precision != LQMC_PREC_FP64E)
@@ -153,12 +153,12 @@ int lqmc_create(const lqmc_params* params, lqmc_handle** out) {
         return fail(nullptr, LQMC_ERR_INVALID, "unknown engine");
     if (params->engine == LQMC_ENGINE_SMEM && params->precision == LQMC_PREC_MIXED)
         return fail(nullptr, LQMC_ERR_UNSUPPORTED, "the shared-memory kernel is float64 only");
-    if (params->engine == LQMC_ENGINE_TILED && params->mode == LQMC_MODE_COMPAT)
-        return fail(nullptr, LQMC_ERR_UNSUPPORTED, "compat mode runs on the shared-memory kernel only");
+    if (params->engine == LQMC_ENGINE_TILED && params->mode != LQMC_MODE_DQMC)
+        return fail(nullptr, LQMC_ERR_UNSUPPORTED, "compat and det modes run on the shared-memory kernel only");
     if (params->stab_every < 0 || params->delay < 0)
         return fail(nullptr, LQMC_ERR_INVALID, "negative stab_every or delay");
-    if (params->precision != LQMC_PREC_FP64 && params->mode == LQMC_MODE_COMPAT)
-        return fail(nullptr, LQMC_ERR_UNSUPPORTED, "compat mode replays float64 arithmetic only");
+    if (params->precision != LQMC_PREC_FP64 && params->mode != LQMC_MODE_DQMC)
+        return fail(nullptr, LQMC_ERR_UNSUPPORTED, "compat and det modes replay float64 arithmetic only");
     if (params->engine == LQMC_ENGINE_SMEM && params->precision == LQMC_PREC_FP64E)
         return fail(nullptr, LQMC_ERR_UNSUPPORTED, "the shared-memory kernel has no emulated GEMM");
     int ndev = 0;
@@ -190,9 +190,9 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
     for (int c = 0; c < n_chains; ++c) {
         if (n_sites[c] < 1 || n_slices[c] < 1)
             return fail(h, LQMC_ERR_INVALID, "chain " + std::to_string(c) + ": n_sites and n_slices must be >= 1");
-        if (h->p.mode == LQMC_MODE_COMPAT && n_sites[c] > kMaxSitesSmem)
+        if (h->p.mode != LQMC_MODE_DQMC && n_sites[c] > kMaxSitesSmem)
             return fail(h, LQMC_ERR_UNSUPPORTED, "chain " + std::to_string(c) +
-                        ": compat mode runs on the shared-memory kernel, n_sites <= 128");
+                        ": compat and det modes run on the shared-memory kernel, n_sites <= 128");
         if (h->p.engine == LQMC_ENGINE_SMEM && n_sites[c] > kMaxSitesSmem)
             return fail(h, LQMC_ERR_UNSUPPORTED, "chain " + std::to_string(c) +
                         ": the shared-memory kernel holds n_sites <= 128");

@@ -104,6 +104,117 @@ __device__ void compat_wrap(const ChainDesc& d, Smem& sm, int l_next) {
 }
 
 // ---------------------------------------------------------------------------------------
+// det mode: the reference's slow path (lqmc.py:236-299), every ratio from determinants
+// ---------------------------------------------------------------------------------------
+
+// log|det W| and sign(det W) by LU with partial pivoting (first maximal |pivot|); W is
+// overwritten.  *singular = 1 on a zero pivot.
+__device__ void lu_logdet(double* w, int n, double* sv, double* logabs, double* sgn, int* singular) {
+    const int lane = lane_id();
+    int* spiv = reinterpret_cast<int*>(sv + kNW);
+    double la = 0.0, sg = 1.0;
+    int sing = 0;
+    for (int j = 0; j < n; ++j) {
+        if (warp_id() == 0) {
+            double best = -1.0;
+            int bi = n;
+            for (int i = j + lane; i < n; i += 32) {
+                const double v = fabs(w[i * n + j]);
+                if (v > best) { best = v; bi = i; }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (lane == 0) *spiv = (bi < n) ? bi : j;   // all-NaN column: keep the row
+        }
+        __syncthreads();
+        const int p = *spiv;
+        if (p != j) {
+            for (int k = threadIdx.x; k < n; k += kNT) {
+                const double t = w[j * n + k]; w[j * n + k] = w[p * n + k]; w[p * n + k] = t;
+            }
+            sg = -sg;
+        }
+        __syncthreads();
+        const double piv = w[j * n + j];
+        if (piv == 0.0) sing = 1;
+        la += log(fabs(piv));
+        if (piv < 0.0) sg = -sg;
+        const int rows = n - j - 1;
+        for (int e = threadIdx.x; e < rows * rows; e += kNT) {
+            const int i = j + 1 + e / rows, k = j + 1 + e % rows;
+            w[i * n + k] = fma(-(w[i * n + j] / piv), w[j * n + k], w[i * n + k]);
+        }
+        __syncthreads();
+    }
+    *logabs = la;
+    *sgn = sg;
+    *singular |= sing;
+}
+
+// M_s = 1 + b_{l0-1} ... b_0 b_{L-1} ... b_{l0}, b_t = exp_k diag(exp_v(t)), the cyclic product
+// of get_m(l0, sigma) (lqmc.py:156-185), factorised for its log|det| and sign
+__device__ void det_m(const ChainDesc& d, Smem& sm, int l0, int s, double* la, double* sg, int* singular) {
+    const int n = d.n, nn = n * n, L = d.L, sigma = s ? -1 : 1;
+    double* x = sm.s1;
+    double* b = sm.s0;
+    for (int k = 0; k < L; ++k) {
+        const int t = ((l0 - 1 - k) % L + L) % L;
+        load_ev(d, sm.ev, t, sigma);
+        __syncthreads();
+        double* dst = k ? b : x;
+        for (int e = threadIdx.x; e < nn; e += kNT) dst[e] = __dmul_rn(d.expk[e], sm.ev[e % n]);
+        __syncthreads();
+        if (k) {
+            gemm_right_inplace(x, b, n);
+            __syncthreads();
+        }
+    }
+    for (int i = threadIdx.x; i < n; i += kNT) x[i * n + i] = __dadd_rn(1.0, x[i * n + i]);
+    __syncthreads();
+    lu_logdet(x, n, sm.sv, la, sg, singular);
+}
+
+// One det-mode sweep (lqmc.py:236-259): flip, recompute det M_up det M_dn, accept with
+// u <= new / old, else flip back.  la_old / sg_old carry the current configuration's
+// log|det M| and sign per spin.
+__device__ void det_sweep(const ChainDesc& d, Smem& sm, int sw, uint64_t sweep_id, double* la_old,
+                          double* sg_old, int* accepted, int* singular) {
+    const int n = d.n, L = d.L;
+    for (int l = L - 1; l >= 0; --l) {
+        int8_t* f = d.field + (size_t)l * n;
+        const int step = L - 1 - l;
+        for (int i = 0; i < n; ++i) {
+            const int pos = step * n + i;
+            if (threadIdx.x == 0) f[i] = (int8_t)(-f[i]);
+            __syncthreads();
+            double la[2], sg[2];
+            det_m(d, sm, l, 0, &la[0], &sg[0], singular);
+            det_m(d, sm, l, 1, &la[1], &sg[1], singular);
+            double u;
+            if (d.rng == LQMC_RNG_REPLAY) u = d.uniforms[(size_t)sw * n * L + pos];
+            else u = philox_uniform(d.seed, (uint64_t)d.chain_id, sweep_id, (uint64_t)pos);
+            const double ratio = (sg[0] * sg[1]) / (sg_old[0] * sg_old[1]) *
+                                 exp((la[0] + la[1]) - (la_old[0] + la_old[1]));
+            const bool acc = (u <= ratio);
+            if (acc) {
+                la_old[0] = la[0]; la_old[1] = la[1];
+                sg_old[0] = sg[0]; sg_old[1] = sg[1];
+            }
+            if (threadIdx.x == 0) {
+                if (acc) ++*accepted;
+                else f[i] = (int8_t)(-f[i]);
+                if (d.record) d.decisions[((size_t)sw * L + step) * n + i] = acc ? 1 : 0;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
 // dqmc mode: UDT chain products
 // ---------------------------------------------------------------------------------------
 
@@ -502,8 +613,27 @@ sweep_fp64_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_meas
         ph[k] += t_ - tc;                   \
         tc = t_;                            \
     } while (0)
+    double la_old[2] = {0.0, 0.0}, sg_old[2] = {1.0, 1.0};   // det mode
     for (int sw = 0; sw < n_sweeps; ++sw, ++sweep_id) {
-        if (d.mode == LQMC_MODE_COMPAT) {
+        if (d.mode == LQMC_MODE_DET) {
+            // det M of the current configuration, recomputed when a launch starts as the
+            // reference does when each of its loops starts (lqmc.py:261-266, :277-282)
+            if (sw == 0) {
+                det_m(d, sm, 0, 0, &la_old[0], &sg_old[0], &singular);
+                det_m(d, sm, 0, 1, &la_old[1], &sg_old[1], &singular);
+            }
+            LQMC_PHASE(0);
+            det_sweep(d, sm, sw, sweep_id, la_old, sg_old, &accepted, &singular);
+            LQMC_PHASE(1);
+            // G = inv(get_m(0, sigma)) for the measurement (lqmc.py:293-295) and the output
+            compat_recompute(d, sm, 0, &singular);
+            compat_recompute(d, sm, 1, &singular);
+            for (int s = 0; s < 2; ++s) {
+                logdet[s] = -la_old[s];
+                sgn[s] = sg_old[s];
+            }
+            LQMC_PHASE(0);
+        } else if (d.mode == LQMC_MODE_COMPAT) {
             compat_recompute(d, sm, 0, &singular);
             compat_recompute(d, sm, 1, &singular);
             LQMC_PHASE(0);

@@ -72,8 +72,9 @@ class ChainSpec:
 class Engine:
     """Batched DQMC sweep engine on one GPU.
 
-    mode       'compat' (reference arithmetic, lqmc/lqmc.py:301-347) or 'dqmc' (textbook,
-               stabilised)
+    mode       'compat' (reference arithmetic, lqmc/lqmc.py:301-347), 'dqmc' (textbook,
+               stabilised) or 'det' (the reference's determinant mode, lqmc/lqmc.py:236-299:
+               every ratio from det M of the flipped configuration; a slow check path)
     precision  'fp64'; 'fp64e' (float64 G and updates, every dense product a float64-accurate
                GEMM emulated on the BF16 tensor cores); or 'mixed' (float32 G, wraps, updates
                and B-chain products; float64 Householder QR and LU of the stabilisation)

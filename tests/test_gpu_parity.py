@@ -204,3 +204,27 @@ def test_determinism_same_seed_bit_identical():
         eng.close()
     for a, b in zip(out[0], out[1]):
         np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", ["det_2x2.npz", "det_4x4.npz"])
+def test_det_mode_replays_reference_det_mode(name):
+    """GPU det mode (lqmc.py:236-299): every decision from determinants of the flipped
+    configuration, identical to the reference's recorded det-mode decisions."""
+    f = golden(name)
+    N, L = int(f["side"]) ** 2, int(f["L"])
+    spec = ChainSpec(f["kinetic"], float(f["u"]), float(f["beta"]), L, f["field0"],
+                     exp_k=f["exp_k"], exp_k_inv=f["exp_k_inv"], consts=f["consts"])
+    eng = Engine([spec], mode="det", rng="replay", record=True)
+    u = f["uniforms"]
+    for sw in range(int(f["n_sweeps"])):
+        eng.set_uniforms(0, u[sw * N * L:(sw + 1) * N * L])
+        eng.sweep(1, measure=True)
+        assert np.array_equal(eng.decisions(0)[0], f["accept"][sw])
+    np.testing.assert_array_equal(eng.field(0), f["field_end"])
+    # G = inv(get_m(0, sigma)) of the final configuration, as the reference measures
+    g = eng.green(0)
+    for s, sigma in enumerate((1, -1)):
+        m = ocompat.get_m(f["exp_k"], f["field_end"], float(f["lamb"]), 0, sigma)
+        np.testing.assert_allclose(g[s], np.linalg.inv(m), rtol=0, atol=1e-9)
+    assert not eng.status().any()
+    eng.close()
