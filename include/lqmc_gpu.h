@@ -115,9 +115,10 @@ typedef struct lqmc_params {
 #define LQMC_FP64E_NATIVE_UDT 4      /* blocked QR updates, Q and T of the UDT factors        */
 #define LQMC_FP64E_NATIVE_GREEN 8    /* U_R^T U_L, T_R T_L^T and U_L Z of the stable inverse   */
 #define LQMC_FP64E_NATIVE_UPDATE 16  /* delayed rank-k updates G -= X Y^T                     */
-#define LQMC_FP64E_NATIVE_LU 32      /* trailing updates of the stabilised inverse's LU (the
-                                        Python Engine's default; emulated, they are equilibrated
-                                        along k and leave a larger stabilisation residual)    */
+#define LQMC_FP64E_NATIVE_LU 32      /* trailing updates of the stabilised inverse's LU
+                                        factorisation (emulated, they are equilibrated along k
+                                        and leave a larger stabilisation residual)             */
+#define LQMC_FP64E_NATIVE_LU_RHS 64  /* the LU solve's updates of its right-hand side          */
 
 /* debug bits (lqmc_params.debug), for testing the failure paths */
 #define LQMC_DEBUG_STALL_TC_WAIT 1  /* emulated-GEMM kernel: the first tensor-core step issues

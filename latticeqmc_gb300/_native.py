@@ -21,7 +21,8 @@ RNGS = {"replay": 0, "philox": 1}
 ENGINES = {"auto": 0, "smem": 1, "tiled": 2}
 STATUS_NONFINITE, STATUS_SINGULAR, STATUS_DRIFT, STATUS_TIMEOUT = 1, 2, 4, 8
 DEBUG_STALL_TC_WAIT = 1
-FP64E_NATIVE = {"wrap": 1, "stack": 2, "udt": 4, "green": 8, "update": 16, "lu": 32}
+FP64E_NATIVE = {"wrap": 1, "stack": 2, "udt": 4, "green": 8, "update": 16, "lu": 32,
+                "lu_rhs": 64}
 OBS_HEADER = 8
 DIAG_LEN = 24
 
@@ -101,7 +102,7 @@ class Handle:
     """Owns one lqmc_handle; every call checks the return code."""
 
     def __init__(self, mode, precision, rng, stab_every, delay, seed, record, device,
-                 engine="auto", debug=0, fp64e_native=("lu",)):
+                 engine="auto", debug=0, fp64e_native=("lu", "lu_rhs")):
         self.lib = load()
         if isinstance(fp64e_native, int):
             native = fp64e_native

@@ -268,7 +268,9 @@ constexpr int kPanel = 32;   // widest panel
 
 __host__ __device__ constexpr int panel_width(int n) { return n <= 256 ? 32 : (n <= 512 ? 16 : 8); }
 
-template <bool EMU>
+// EMU_W / EMU_R: the factorisation's trailing updates / the right-hand side's updates on the
+// emulated GEMM (else the float64 tiled GEMM)
+template <bool EMU_W, bool EMU_R>
 __device__ void lu_solve_blocked(TSmem<double>& sm, double* w, double* rhs, int n, double* panel,
                                  int* piv, double* sv, double* logabs, double* sgn, int* singular) {
     const int lane = lane_id();
@@ -357,12 +359,12 @@ __device__ void lu_solve_blocked(TSmem<double>& sm, double* w, double* rhs, int 
             o.subtract = true;
             o.kscale = true;
             // W22 -= L21 U12 ; R2 -= L21 R1
-            gemm_t<double, EMU, 0, false, false>(sm, w + (size_t)(jb + nb) * n + jb + nb, n,
-                                              w + (size_t)(jb + nb) * n + jb, n,
-                                              w + (size_t)jb * n + jb + nb, n, rest, rest, nb, o);
-            gemm_t<double, EMU, 0, false, false>(sm, rhs + (size_t)(jb + nb) * n, n,
-                                              w + (size_t)(jb + nb) * n + jb, n,
-                                              rhs + (size_t)jb * n, n, rest, n, nb, o);
+            gemm_t<double, EMU_W, 0, false, false>(sm, w + (size_t)(jb + nb) * n + jb + nb, n,
+                                                w + (size_t)(jb + nb) * n + jb, n,
+                                                w + (size_t)jb * n + jb + nb, n, rest, rest, nb, o);
+            gemm_t<double, EMU_R, 0, false, false>(sm, rhs + (size_t)(jb + nb) * n, n,
+                                                w + (size_t)(jb + nb) * n + jb, n,
+                                                rhs + (size_t)jb * n, n, rest, n, nb, o);
         }
     }
     // back substitution with U, 32-row blocks from the bottom
@@ -384,7 +386,7 @@ __device__ void lu_solve_blocked(TSmem<double>& sm, double* w, double* rhs, int 
             o.subtract = true;
             o.kscale = true;
             // R0 -= U01 R1
-            gemm_t<double, EMU, 0, false, false>(sm, rhs, n, w + jb, n, rhs + (size_t)jb * n, n, jb, n, nb, o);
+            gemm_t<double, EMU_R, 0, false, false>(sm, rhs, n, w + jb, n, rhs + (size_t)jb * n, n, jb, n, nb, o);
         }
     }
     *logabs = la;
@@ -400,7 +402,7 @@ __device__ void lu_solve_dispatch(TSmem<T>& sm, int n, double* la, double* sw, i
 
 template <>
 __device__ void lu_solve_dispatch<double, false>(TSmem<double>& sm, int n, double* la, double* sw, int* sing) {
-    lu_solve_blocked<false>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
+    lu_solve_blocked<false, false>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
 }
 // The stabilised matrix is graded in its rows and columns, so L21 and U12 (and U01, R1 of the
 // back substitution) carry mirrored grading along the contraction index; the emulated
@@ -408,10 +410,11 @@ __device__ void lu_solve_dispatch<double, false>(TSmem<double>& sm, int n, doubl
 // accuracy relative to each row / column.  LQMC_FP64E_NATIVE_LU keeps them in float64.
 template <>
 __device__ void lu_solve_dispatch<double, true>(TSmem<double>& sm, int n, double* la, double* sw, int* sing) {
-    if (sm.native & LQMC_FP64E_NATIVE_LU)
-        lu_solve_blocked<false>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
-    else
-        lu_solve_blocked<true>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
+    const bool nw = sm.native & LQMC_FP64E_NATIVE_LU, nr = sm.native & LQMC_FP64E_NATIVE_LU_RHS;
+    if (nw && nr) lu_solve_blocked<false, false>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
+    else if (nw) lu_solve_blocked<false, true>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
+    else if (nr) lu_solve_blocked<true, false>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
+    else lu_solve_blocked<true, true>(sm, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
 }
 template <>
 __device__ void lu_solve_dispatch<float, false>(TSmem<float>& sm, int n, double* la, double* sw, int* sing) {
@@ -419,7 +422,7 @@ __device__ void lu_solve_dispatch<float, false>(TSmem<float>& sm, int n, double*
     TSmem<double> d;
     d.stage = sm.stage64;
     d.oz = sm.oz;
-    lu_solve_blocked<false>(d, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
+    lu_solve_blocked<false, false>(d, sm.s0, sm.s1, n, sm.panel, sm.piv, sm.sv, la, sw, sing);
 }
 
 // Float64 GEMM of the QR: the emulated tensor-core GEMM, or the float64 tiled GEMM on the

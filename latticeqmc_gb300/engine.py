@@ -82,14 +82,15 @@ class Engine:
     engine     'auto', 'smem' (one CTA per chain, G in shared memory, fp64, N <= 128) or
                'tiled' (matrices in global memory, tiled GEMMs; any N up to 2048)
     fp64e_native  product categories the fp64e engine keeps in native float64: names from
-               'wrap', 'stack', 'udt', 'green', 'update', 'lu' (or an LQMC_FP64E_NATIVE_* mask).
-               Default ('lu',): the stabilised inverse's LU in float64 (its k-scaled emulated
-               form is ~3 % faster at 16x16, beta=8 but leaves a larger stabilisation residual)
+               'wrap', 'stack', 'udt', 'green', 'update', 'lu', 'lu_rhs' (or an
+               LQMC_FP64E_NATIVE_* mask).  Default ('lu', 'lu_rhs'): the stabilised inverse's LU
+               solve in float64 (emulating its right-hand-side updates is ~5 % faster at 16x16,
+               beta=8, but leaves a 7x larger median stabilisation residual)
     """
 
     def __init__(self, chains, mode="dqmc", precision="fp64", rng="philox", stab_every=None,
                  delay=0, seed=0, record=False, device=0, engine="auto", debug=0,
-                 fp64e_native=("lu",)):
+                 fp64e_native=("lu", "lu_rhs")):
         self.chains = list(chains)
         if stab_every is None:
             stab_every = auto_stab_every(self.chains)

@@ -202,7 +202,7 @@ def test_fp64e_with_every_category_native_is_the_fp64_engine():
     a = Engine([spec], mode="dqmc", precision="fp64", engine="tiled", rng="replay", stab_every=5,
                delay=16)
     b = Engine([spec], mode="dqmc", precision="fp64e", rng="replay", stab_every=5, delay=16,
-               fp64e_native=("wrap", "stack", "udt", "green", "update", "lu"))
+               fp64e_native=("wrap", "stack", "udt", "green", "update", "lu", "lu_rhs"))
     for e in (a, b):
         e.set_uniforms(0, u)
         e.sweep(1)
