@@ -524,10 +524,14 @@ __device__ void oz_gemm_tc(double* c, int ldc, const double* a, int lda, const d
             const bool magic_ok = steps * kBK * 8 * 64 * 64 < (1 << 22);
 #pragma unroll 1
             for (int h = 0; h < 2; ++h) {
+                if (j0 + 32 * h >= n) break;   // the whole half lies outside C (uniform)
 #pragma unroll 1
                 for (int g = 0; g < 2; ++g) {
                     const int cl = 16 * (w >> 2) + 8 * g;   // column within the half
                     const int ct = 32 * h + cl;             // column within the tile
+                    // a warp whose 32 rows or 8 columns all lie outside C skips them (the
+                    // condition is uniform over the warp, as the collective TMEM load needs)
+                    if (j0 + ct >= n || i0 + 32 * (w & 3) >= m) continue;
                     int ej[8];
 #pragma unroll
                     for (int x = 0; x < 8; ++x) ej[x] = (j0 + ct + x < n) ? eb[j0 + ct + x] : 0;

@@ -219,12 +219,13 @@ __device__ void panel_v(double* v, const double* s, int n, int jb, int b) {
 
 // T factor of the compact WY form H_jb ... H_{jb+b-1} = I - V T V^T (LAPACK dlarft, forward,
 // columnwise): T(i, i) = tau_i, T(0:i, i) = -tau_i T(0:i, 0:i) (V^T V)(0:i, i).  gram is V^T V
-// and tf the b x b row-major T (b <= 32: one lane per row).
+// and tf the b x b row-major T (b <= 64: one warp, lane r owns rows r and r + 32; a row only
+// reads its own earlier entries).
 __device__ void wy_t_factor(double* tf, const double* gram, const double* tau, int b) {
     if (warp_id() == 0) {
-        const int r = lane_id();
+        const int lane = lane_id();
         for (int i = 0; i < b; ++i) {
-            if (r < b) {
+            for (int r = lane; r < b; r += 32) {
                 double v = 0.0;
                 if (r < i) {
                     for (int q = r; q < i; ++q) v = fma(tf[r * b + q], gram[q * b + i], v);
@@ -240,9 +241,22 @@ __device__ void wy_t_factor(double* tf, const double* gram, const double* tau, i
     __syncthreads();
 }
 
-// panel width of the blocked QR; with bw <= n / 5 the scratch of udt_absorb_t
-// (ceil((n - 1) / bw) bw^2 + 3 n bw doubles) fits in the n^2 of S1
-__device__ __forceinline__ int qr_block(int n) { return min(32, max(1, n / 5)); }
+#ifndef LQMC_QR_BLOCK_MAX
+#define LQMC_QR_BLOCK_MAX 64
+#endif
+
+// scratch doubles of udt_absorb_t for panel width bw: the panels' T factors and V, V T, V^T C
+__device__ __forceinline__ size_t qr_scratch(int n, int bw) {
+    return (size_t)((n - 2) / bw + 1) * bw * bw + 3 * (size_t)n * bw;
+}
+
+// panel width of the blocked QR: the widest <= LQMC_QR_BLOCK_MAX (at most 64, the limit of
+// wy_t_factor) whose scratch fits in the n^2 of S1
+__device__ __forceinline__ int qr_block(int n) {
+    int bw = min(min(LQMC_QR_BLOCK_MAX, 64), max(1, n / 4));
+    while (bw > 1 && qr_scratch(n, bw) > (size_t)n * n) --bw;
+    return bw;
+}
 
 // Solve W Z = R in place (both n x n, row-major, global memory) by a blocked right-looking
 // bytes of the GEMM staging region: the kernel's own GEMM (tiled T, or emulated with
