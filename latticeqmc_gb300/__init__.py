@@ -15,7 +15,7 @@ from .engine import ChainSpec, Engine
 from .hubbard import HubbardModel
 from .lattice import Lattice
 from .lqmc import LatticeQMC
-from .scan import scan
+from .scans import scan
 from .tools import (check_params, compute_pole_gf_tau, fermi_fct, filling, local_gf,
                     local_moment, matsubara_frequencies, pole_gf_tau)
 
