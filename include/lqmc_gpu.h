@@ -106,7 +106,9 @@ typedef struct lqmc_params {
     int32_t debug;         /* LQMC_DEBUG_* bits; 0 in production                           */
     int32_t fp64e_native;  /* LQMC_FP64E_NATIVE_* bits: product categories the fp64e engine
                               keeps in native float64 (0: all on the tensor cores)            */
-    int32_t reserved[4];
+    int32_t measure_tau;   /* 1: measured sweeps also accumulate the unequal-time G(tau_l, 0)
+                              of every slice (LQMC_MODE_DQMC only; lqmc_get_green_tau)      */
+    int32_t reserved[3];
 } lqmc_params;
 
 /* product categories of the fp64e engine (lqmc_params.fp64e_native) */
@@ -203,6 +205,23 @@ int lqmc_get_diagnostics(lqmc_handle* h, int32_t chain, double* diag);
  * cannot be resumed); serves the per-chain checkpoint / resume of long beta / U scans. */
 int lqmc_set_chain_state(lqmc_handle* h, int32_t chain, const double* diag, const double* green_sum,
                          const double* obs);
+
+/* Unequal-time Green's function (params.measure_tau = 1): the sum over the measured sweeps
+ * of G_sigma(tau_l, 0) = B_{l-1} ... B_0 (1 + B_{L-1} ... B_0)^-1, B_l = exp(V_sigma(l))
+ * exp(-dtau K), for l = 0 .. L-1 (tau_l = l dtau), of the field each measured sweep ends
+ * with; float64 [2][L][N][N]; divide by the measurement count (observables[0]).
+ * G(tau, 0) = <c_i(tau) c_j^+(0)>, i.e. minus the imaginary-time Green's function that
+ * lqmc/tools.py:182-200 (compute_pole_gf_tau) gives at U = 0.  The end-of-sweep G that
+ * lqmc_get_green_sum accumulates is the equal-time G at tau_1 (the slice boundary above
+ * slice 0): per sample G(tau_1, 0) = G_sweep B_0.  Stabilised: recomputed from UDT factors
+ * of B(tau, 0) and B(beta, tau) at every multiple of stab_every and propagated one slice at
+ * a time in between.  No reference counterpart in the solver (it measures only the
+ * equal-time G, lqmc/lqmc.py:356-375). */
+int lqmc_get_green_tau(lqmc_handle* h, int32_t chain, double* green_tau_sum);
+
+/* Restore a chain's G(tau) sum ([2][L][N][N], as lqmc_get_green_tau returned it), for
+ * checkpoint / resume. */
+int lqmc_set_green_tau(lqmc_handle* h, int32_t chain, const double* green_tau_sum);
 
 /* Per-chain LQMC_STATUS_* bit masks, n_chains int32 (0 = healthy). */
 int lqmc_get_status(lqmc_handle* h, int32_t* status);

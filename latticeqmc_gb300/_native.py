@@ -36,7 +36,7 @@ class Params(ctypes.Structure):
                 ("stab_every", ctypes.c_int32), ("delay", ctypes.c_int32), ("record", ctypes.c_int32),
                 ("seed", ctypes.c_uint64), ("device", ctypes.c_int32), ("engine", ctypes.c_int32),
                 ("debug", ctypes.c_int32), ("fp64e_native", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 4)]
+                ("measure_tau", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
 
 class LqmcError(RuntimeError):
@@ -67,6 +67,8 @@ _SIGS = [
     ("lqmc_get_decisions", ctypes.c_int, [_P, _I32, _P, ctypes.c_size_t]),
     ("lqmc_get_diagnostics", ctypes.c_int, [_P, _I32, _P]),
     ("lqmc_set_chain_state", ctypes.c_int, [_P, _I32, _P, _P, _P]),
+    ("lqmc_get_green_tau", ctypes.c_int, [_P, _I32, _P]),
+    ("lqmc_set_green_tau", ctypes.c_int, [_P, _I32, _P]),
     ("lqmc_get_status", ctypes.c_int, [_P, _P]),
     ("lqmc_get_launch_count", ctypes.c_int, [_P, _P]),
     ("lqmc_last_error", ctypes.c_char_p, [_P]),
@@ -102,7 +104,7 @@ class Handle:
     """Owns one lqmc_handle; every call checks the return code."""
 
     def __init__(self, mode, precision, rng, stab_every, delay, seed, record, device,
-                 engine="auto", debug=0, fp64e_native=("lu", "lu_rhs")):
+                 engine="auto", debug=0, fp64e_native=("lu", "lu_rhs"), measure_tau=False):
         self.lib = load()
         if isinstance(fp64e_native, int):
             native = fp64e_native
@@ -115,7 +117,8 @@ class Handle:
         p = Params(mode=MODES[mode], precision=PRECISIONS[precision], rng=RNGS[rng],
                    stab_every=int(stab_every), delay=int(delay), record=int(bool(record)),
                    seed=int(seed) & ((1 << 64) - 1), device=int(device), engine=ENGINES[engine],
-                   debug=int(debug), fp64e_native=int(native))
+                   debug=int(debug), fp64e_native=int(native),
+                   measure_tau=int(bool(measure_tau)))
         h = ctypes.c_void_p()
         rc = self.lib.lqmc_create(ctypes.byref(p), ctypes.byref(h))
         if rc != LQMC_OK:

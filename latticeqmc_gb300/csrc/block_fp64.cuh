@@ -132,6 +132,31 @@ __device__ inline void gemm(double* __restrict__ c, const double* a, const doubl
     }
 }
 
+// C = op(A) op(B), out of place, any n: the columns in blocks of 32 kMaxRows per warp row.
+// For n <= 32 kMaxRows it performs the same fma chains as gemm<TA, TB>.
+template <bool TA, bool TB>
+__device__ inline void gemm_any(double* __restrict__ c, const double* a, const double* b, int n) {
+    const int lane = lane_id();
+    for (int j0 = 0; j0 < n; j0 += 32 * kMaxRows) {
+        for (int i = warp_id(); i < n; i += kNW) {
+            double acc[kMaxRows] = {0.0, 0.0, 0.0, 0.0};
+            for (int m = 0; m < n; ++m) {
+                const double am = TA ? a[m * n + i] : a[i * n + m];
+#pragma unroll
+                for (int r = 0; r < kMaxRows; ++r) {
+                    const int j = j0 + lane + 32 * r;
+                    if (j < n) acc[r] = fma(am, TB ? b[j * n + m] : b[m * n + j], acc[r]);
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < kMaxRows; ++r) {
+                const int j = j0 + lane + 32 * r;
+                if (j < n) c[i * n + j] = acc[r];
+            }
+        }
+    }
+}
+
 // Solve W Z = R in place by LU with partial pivoting (first maximal |pivot|, like LAPACK
 // idamax).  On return rhs holds Z and w its LU factors.  Returns log|det W| through
 // *logabs (thread-uniform) and sign(det W) through *sgn; *singular = 1 on a zero pivot.

@@ -15,13 +15,16 @@
 namespace lqmc {
 size_t sweep_fp64_smem_bytes(int n, int flags);
 cudaError_t launch_sweep_fp64(const ChainDesc* d_descs, int n_chains, size_t smem, int n_sweeps,
-                              int measure, cudaStream_t stream);
+                              int measure, int sweep_base, cudaStream_t stream);
+size_t green_tau_smem_bytes(int n, int tau_flags);
+size_t green_tau_work_doubles(int n, int n_chunks, int slot, int tau_flags);
+cudaError_t launch_green_tau(const ChainDesc* d_descs, int n_chains, size_t smem, cudaStream_t stream);
 size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu, int stages, bool xy_global);
 int sweep_tiled_delay_target(bool fp32, int requested, bool emu);
 int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap, bool emu, int stages);
 size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32, bool emu, int xy_delay);
 cudaError_t launch_sweep_tiled(const ChainDesc* d_descs, int n_chains, size_t smem, int precision,
-                               int n_sweeps, int measure, cudaStream_t stream);
+                               int n_sweeps, int measure, int sweep_base, cudaStream_t stream);
 }  // namespace lqmc
 
 using lqmc::ChainDesc;
@@ -40,6 +43,7 @@ std::string g_create_error;
 struct Bucket {
     int kind = kSmemFp64;
     size_t smem = 0;
+    size_t tau_smem = 0;   // green_tau_kernel (params.measure_tau)
     std::vector<int> chains;
     ChainDesc* d_descs = nullptr;
     cudaStream_t stream = nullptr;
@@ -161,6 +165,10 @@ int lqmc_create(const lqmc_params* params, lqmc_handle** out) {
         return fail(nullptr, LQMC_ERR_UNSUPPORTED, "compat and det modes replay float64 arithmetic only");
     if (params->engine == LQMC_ENGINE_SMEM && params->precision == LQMC_PREC_FP64E)
         return fail(nullptr, LQMC_ERR_UNSUPPORTED, "the shared-memory kernel has no emulated GEMM");
+    if (params->measure_tau != 0 && params->measure_tau != 1)
+        return fail(nullptr, LQMC_ERR_INVALID, "measure_tau must be 0 or 1");
+    if (params->measure_tau && params->mode != LQMC_MODE_DQMC)
+        return fail(nullptr, LQMC_ERR_UNSUPPORTED, "the unequal-time G is measured in dqmc mode only");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess) return fail(nullptr, LQMC_ERR_CUDA, std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e));
@@ -286,9 +294,20 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
             if (smem[c] > smem_cap) { release(h); return fail(h, LQMC_ERR_UNSUPPORTED, "lattice too large for shared memory"); }
         }
         const size_t fcopy = (kind[c] == kTiledFp32) ? 2 * round_up((nn + 1) / 2, kAlign) : 0;
+        size_t tau = 0;
+        d.tau_flags = 0;
+        if (h->p.measure_tau) {
+            if (lqmc::green_tau_smem_bytes(n, 0) > smem_cap) d.tau_flags = lqmc::kScratchInGlobal;
+            if (lqmc::green_tau_smem_bytes(n, d.tau_flags) > smem_cap) {
+                release(h);
+                return fail(h, LQMC_ERR_UNSUPPORTED, "lattice too large for the unequal-time G kernel");
+            }
+            tau = round_up(2 * (size_t)L * nn, kAlign) +
+                  round_up(lqmc::green_tau_work_doubles(n, d.n_chunks, d.slot, d.tau_flags), kAlign);
+        }
         const size_t need = round_up(nn, kAlign) * 5 + fcopy + round_up(2 * nn, kAlign) +
                             round_up(LQMC_OBS_LEN(n), kAlign) + round_up(LQMC_DIAG_LEN, kAlign) +
-                            round_up(work, kAlign);
+                            tau + round_up(work, kAlign);
         off[c] = total;
         total += need;
         off_i8[c] = total_i8;
@@ -329,6 +348,12 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
         d.gsum = take(2 * nn);
         d.obs = take(LQMC_OBS_LEN(n));
         d.diag = take(LQMC_DIAG_LEN);
+        d.gtau = nullptr;
+        d.tau_work = nullptr;
+        if (h->p.measure_tau) {
+            d.gtau = take(2 * (size_t)d.L * nn);
+            d.tau_work = take(lqmc::green_tau_work_doubles(n, d.n_chunks, d.slot, d.tau_flags));
+        }
         d.work = p;
         d.expk = ek;
         d.expkT = ekt;
@@ -367,6 +392,7 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
         b.kind = (int)kv.first.second;
         b.smem = smem[kv.second[0]];
         b.chains = kv.second;
+        if (h->p.measure_tau) b.tau_smem = lqmc::green_tau_smem_bytes(h->desc[b.chains[0]].n, h->desc[b.chains[0]].tau_flags);
         e = cudaMalloc(&b.d_descs, sizeof(ChainDesc) * b.chains.size());
         if (e != cudaSuccess) { h->buckets.push_back(b); release(h); return fail(h, LQMC_ERR_NOMEM, "descriptor allocation failed"); }
         e = cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking);
@@ -520,24 +546,37 @@ int lqmc_sweep(lqmc_handle* h, int32_t n_sweeps, int32_t measure, void* stream_p
         }
         h->descs_dirty = false;
     }
-    auto launch = [&](Bucket& b, cudaStream_t st) {
-        if (b.kind == kSmemFp64)
-            return lqmc::launch_sweep_fp64(b.d_descs, (int)b.chains.size(), b.smem, n_sweeps, measure, st);
-        const int prec = b.kind == kTiledFp32 ? 1 : (b.kind == kTiledFp64e ? 2 : 0);
-        return lqmc::launch_sweep_tiled(b.d_descs, (int)b.chains.size(), b.smem, prec, n_sweeps,
-                                        measure, st);
-    };
-    if (h->buckets.size() == 1) {
-        LQMC_CK(h, launch(h->buckets[0], stream));
+    // with the unequal-time G measured, one sweep per launch, each followed by the G(tau)
+    // kernel on the field and G it left; else one launch runs every sweep
+    const bool tau = measure && h->p.measure_tau;
+    const int per_launch = tau ? 1 : n_sweeps;
+    auto launch = [&](Bucket& b, cudaStream_t st, int base) {
+        cudaError_t e;
+        const int nc = (int)b.chains.size();
+        if (b.kind == kSmemFp64) {
+            e = lqmc::launch_sweep_fp64(b.d_descs, nc, b.smem, per_launch, measure, base, st);
+        } else {
+            const int prec = b.kind == kTiledFp32 ? 1 : (b.kind == kTiledFp64e ? 2 : 0);
+            e = lqmc::launch_sweep_tiled(b.d_descs, nc, b.smem, prec, per_launch, measure, base, st);
+        }
         ++h->launches;
-    } else {
-        LQMC_CK(h, cudaEventRecord(h->fork, stream));
-        for (auto& b : h->buckets) {
-            LQMC_CK(h, cudaStreamWaitEvent(b.stream, h->fork, 0));
-            LQMC_CK(h, launch(b, b.stream));
-            LQMC_CK(h, cudaEventRecord(b.done, b.stream));
-            LQMC_CK(h, cudaStreamWaitEvent(stream, b.done, 0));
+        if (e == cudaSuccess && tau) {
+            e = lqmc::launch_green_tau(b.d_descs, nc, b.tau_smem, st);
             ++h->launches;
+        }
+        return e;
+    };
+    for (int base = 0; base < n_sweeps; base += per_launch) {
+        if (h->buckets.size() == 1) {
+            LQMC_CK(h, launch(h->buckets[0], stream, base));
+        } else {
+            LQMC_CK(h, cudaEventRecord(h->fork, stream));
+            for (auto& b : h->buckets) {
+                LQMC_CK(h, cudaStreamWaitEvent(b.stream, h->fork, 0));
+                LQMC_CK(h, launch(b, b.stream, base));
+                LQMC_CK(h, cudaEventRecord(b.done, b.stream));
+                LQMC_CK(h, cudaStreamWaitEvent(stream, b.done, 0));
+            }
         }
     }
     if (h->p.rng == LQMC_RNG_REPLAY)
@@ -600,6 +639,7 @@ int lqmc_reset_measurements(lqmc_handle* h) {
     for (auto& d : h->desc) {
         LQMC_CK(h, cudaMemset(d.gsum, 0, 2 * (size_t)d.n * d.n * sizeof(double)));
         LQMC_CK(h, cudaMemset(d.obs, 0, LQMC_OBS_LEN(d.n) * sizeof(double)));
+        if (d.gtau) LQMC_CK(h, cudaMemset(d.gtau, 0, 2 * (size_t)d.L * d.n * d.n * sizeof(double)));
     }
     return LQMC_OK;
 }
@@ -633,6 +673,30 @@ int lqmc_set_chain_state(lqmc_handle* h, int32_t chain, const double* diag, cons
         if (!(obs[0] >= 0.0)) return fail(h, LQMC_ERR_INVALID, "observables[0] (measurement count) must be >= 0");
         LQMC_CK(h, cudaMemcpy(d.obs, obs, LQMC_OBS_LEN(d.n) * sizeof(double), cudaMemcpyHostToDevice));
     }
+    return LQMC_OK;
+}
+
+int lqmc_get_green_tau(lqmc_handle* h, int32_t chain, double* green_tau_sum) {
+    int rc = check_chain(h, chain);
+    if (rc) return rc;
+    if (!green_tau_sum) return fail(h, LQMC_ERR_INVALID, "null output");
+    const ChainDesc& d = h->desc[chain];
+    if (!d.gtau) return fail(h, LQMC_ERR_STATE, "the unequal-time G is not measured (params.measure_tau = 0)");
+    if ((rc = sync_last(h))) return rc;
+    LQMC_CK(h, cudaMemcpy(green_tau_sum, d.gtau, 2 * (size_t)d.L * d.n * d.n * sizeof(double),
+                          cudaMemcpyDeviceToHost));
+    return LQMC_OK;
+}
+
+int lqmc_set_green_tau(lqmc_handle* h, int32_t chain, const double* green_tau_sum) {
+    int rc = check_chain(h, chain);
+    if (rc) return rc;
+    if (!green_tau_sum) return fail(h, LQMC_ERR_INVALID, "null input");
+    const ChainDesc& d = h->desc[chain];
+    if (!d.gtau) return fail(h, LQMC_ERR_STATE, "the unequal-time G is not measured (params.measure_tau = 0)");
+    if ((rc = sync_last(h))) return rc;
+    LQMC_CK(h, cudaMemcpy(d.gtau, green_tau_sum, 2 * (size_t)d.L * d.n * d.n * sizeof(double),
+                          cudaMemcpyHostToDevice));
     return LQMC_OK;
 }
 

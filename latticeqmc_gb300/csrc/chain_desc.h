@@ -46,6 +46,10 @@ struct ChainDesc {
     int32_t oz_stages;        // tiled kernel, emulated GEMMs: tensor-core stage buffers (1 or 2)
     int32_t debug;            // LQMC_DEBUG_* bits
     int32_t native;           // LQMC_FP64E_NATIVE_* bits (emulated-GEMM kernel)
+    double* gtau;             // [2][L][n][n] measurement sum of G(tau_l, 0), or null
+    double* tau_work;         // per spin: (n_chunks + 1) UDT slots, then X (+ scratch)
+    int32_t tau_flags;        // kScratchInGlobal: the G(tau) kernel's two scratch matrices
+    int32_t tau_pad;
 };
 
 }  // namespace lqmc

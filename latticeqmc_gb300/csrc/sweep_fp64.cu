@@ -567,10 +567,87 @@ __device__ void measure(const ChainDesc& d, Smem& sm) {
     __syncthreads();
 }
 
+// ---------------------------------------------------------------------------------------
+// Unequal-time G(tau_l, 0) = B_{l-1} ... B_0 G(0) (dqmc mode's B_l = exp_v(l) exp_k)
+// ---------------------------------------------------------------------------------------
+
+// X = G(tau, 0) = B(tau, 0) (1 + B(beta, tau) B(tau, 0))^-1 from the UDT factors
+// B(tau, 0) = U_R D_R T_R and B(beta, tau)^T = U_L D_L T_L.  With D = D_big D_small on each
+// side and the equal-time matrix W = D_bigR^-1 U_R^T U_L D_bigL^-1 + D_smallR T_R T_L^T
+// D_smallL, G(tau) = U_L D_bigL^-1 W^-1 D_bigR^-1 U_R^T, and G(tau, 0) = G(tau) B(tau, 0)
+// = U_L D_bigL^-1 W^-1 D_smallR T_R: no factor above 1 is left outside the solve.
+// ur == nullptr: B(tau, 0) is the identity (tau = 0), X = U_L D_bigL^-1 W^-1.
+__device__ void green_tau_udt(const ChainDesc& d, Smem& sm, const double* ur, const double* dr,
+                              const double* tr, const double* ul, const double* dl,
+                              const double* tl, double* x, int* singular) {
+    const int n = d.n, nn = n * n;
+    double* dbr = sm.xv[0];
+    double* dsr = sm.xv[1];
+    double* dbl = sm.yv[0];
+    double* dsl = sm.yv[1];
+    for (int i = threadIdx.x; i < n; i += kNT) {
+        const double a = ur ? dr[i] : 1.0, b = fmax(fabs(a), 1.0);
+        dbr[i] = b;
+        dsr[i] = a / b;
+        const double c = dl[i], e = fmax(fabs(c), 1.0);
+        dbl[i] = e;
+        dsl[i] = c / e;
+    }
+    if (ur) {
+        gemm_any<true, false>(sm.s0, ur, ul, n);   // U_R^T U_L
+        gemm_any<false, true>(sm.s1, tr, tl, n);   // T_R T_L^T
+    } else {
+        for (int e = threadIdx.x; e < nn; e += kNT) {
+            sm.s0[e] = ul[e];
+            sm.s1[e] = tl[(e % n) * n + e / n];
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nn; e += kNT) {
+        const int i = e / n, j = e % n;
+        sm.s0[e] = sm.s0[e] / dbr[i] / dbl[j] + dsr[i] * sm.s1[e] * dsl[j];
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nn; e += kNT)
+        sm.s1[e] = ur ? dsr[e / n] * tr[e] : ((e / n == e % n) ? 1.0 : 0.0);
+    __syncthreads();
+    double la, sw;
+    int sing;
+    lu_solve(sm.s0, sm.s1, n, sm.sv, &la, &sw, &sing);
+    if (sing) *singular = 1;
+    for (int e = threadIdx.x; e < nn; e += kNT) sm.s1[e] = sm.s1[e] / dbl[e / n];
+    __syncthreads();
+    gemm_any<false, false>(x, ul, sm.s1, n);
+    __syncthreads();
+}
+
+// z <- B_l z = exp_v(l) (exp_k z), through the scratch `tmp`
+__device__ void tau_b_left(const ChainDesc& d, Smem& sm, double* z, double* tmp, int l, int sigma) {
+    const int n = d.n, nn = n * n;
+    __syncthreads();
+    gemm_any<false, false>(tmp, d.expk, z, n);
+    load_ev(d, sm.ev, l, sigma);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nn; e += kNT) z[e] = sm.ev[e / n] * tmp[e];
+    __syncthreads();
+}
+
+// z <- B_l^T z = exp_k^T (exp_v(l) z), through the scratch `tmp`
+__device__ void tau_bt_left(const ChainDesc& d, Smem& sm, double* z, double* tmp, int l, int sigma) {
+    const int n = d.n, nn = n * n;
+    load_ev(d, sm.ev, l, sigma);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nn; e += kNT) tmp[e] = sm.ev[e / n] * z[e];
+    __syncthreads();
+    gemm_any<true, false>(z, d.expk, tmp, n);
+    __syncthreads();
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(kNT, 1)
-sweep_fp64_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_measure) {
+sweep_fp64_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_measure,
+                  int sweep_base) {
     extern __shared__ __align__(16) double smem[];
     __shared__ ChainDesc d;
     __shared__ int accepted;
@@ -614,11 +691,12 @@ sweep_fp64_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_meas
         tc = t_;                            \
     } while (0)
     double la_old[2] = {0.0, 0.0}, sg_old[2] = {1.0, 1.0};   // det mode
-    for (int sw = 0; sw < n_sweeps; ++sw, ++sweep_id) {
+    // sw indexes the call's uniforms and decisions: sweep_base + the sweep of this launch
+    for (int sw = sweep_base; sw < sweep_base + n_sweeps; ++sw, ++sweep_id) {
         if (d.mode == LQMC_MODE_DET) {
             // det M of the current configuration, recomputed when a launch starts as the
             // reference does when each of its loops starts (lqmc.py:261-266, :277-282)
-            if (sw == 0) {
+            if (sw == sweep_base) {
                 det_m(d, sm, 0, 0, &la_old[0], &sg_old[0], &singular);
                 det_m(d, sm, 0, 1, &la_old[1], &sg_old[1], &singular);
             }
@@ -715,13 +793,111 @@ size_t sweep_fp64_smem_bytes(int n, int flags) {
 }
 
 cudaError_t launch_sweep_fp64(const ChainDesc* d_descs, int n_chains, size_t smem, int n_sweeps,
-                              int measure, cudaStream_t stream) {
+                              int measure, int sweep_base, cudaStream_t stream) {
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(sweep_fp64_kernel,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    sweep_fp64_kernel<<<n_chains, kNT, smem, stream>>>(d_descs, n_sweeps, measure);
+    sweep_fp64_kernel<<<n_chains, kNT, smem, stream>>>(d_descs, n_sweeps, measure, sweep_base);
+    return cudaGetLastError();
+}
+
+// G(tau_l, 0) = B(tau_l, 0) (1 + B(beta, 0))^-1, l = 0 .. L-1, of the field the last sweep
+// left, added to desc.gtau.  One CTA per (chain, spin); float64 for every engine.
+//   1. B(beta, tau_c)^T, tau_c = c stab_every, c = nc-1 .. 0, as UDT factors (slot c),
+//      built down from the top like the sweep's left products;
+//   2. at every chunk start X = G(tau_c, 0) from the UDT factors of B(tau_c, 0) (ping-pong
+//      slots nc, nc+1, built up from the bottom like the sweep's right stack) and of
+//      B(beta, tau_c) (green_tau_udt); inside the chunk X <- B_l X slice by slice.
+__global__ void __launch_bounds__(kNT, 1) green_tau_kernel(const ChainDesc* __restrict__ descs) {
+    extern __shared__ __align__(16) double smem[];
+    __shared__ ChainDesc d;
+    __shared__ int singular;
+    const int s = blockIdx.y, sigma = s ? -1 : 1;
+    if (threadIdx.x == 0) {
+        d = descs[blockIdx.x];
+        singular = 0;
+        const size_t nn = (size_t)d.n * d.n;
+        const size_t per_spin = (size_t)(d.n_chunks + 2) * d.slot + nn +
+                                ((d.tau_flags & kScratchInGlobal) ? 2 * nn : 0);
+        d.work = d.tau_work + (size_t)s * per_spin;   // slot_u(d, k): this spin's slot k
+    }
+    __syncthreads();
+    const int n = d.n, nn = n * n, L = d.L, nc = d.n_chunks, se = d.stab_every;
+    Smem sm;
+    double* p = smem;
+    sm.sv = p; p += kNW + 8;
+    sm.xv[0] = p; p += n;
+    sm.xv[1] = p; p += n;
+    sm.yv[0] = p; p += n;
+    sm.yv[1] = p; p += n;
+    sm.ev = p; p += n;
+    sm.nrm = p; p += n;
+    sm.tau = p; p += n;
+    sm.dv = p; p += n;
+    sm.order = reinterpret_cast<int*>(p); p += n;
+    p = smem + (((p - smem) + 3) & ~(ptrdiff_t)3);
+    sm.g[0] = sm.g[1] = nullptr;
+    double* x = d.work + (size_t)(nc + 2) * d.slot;
+    if (d.tau_flags & kScratchInGlobal) { sm.s0 = x + nn; sm.s1 = x + 2 * nn; }
+    else { sm.s0 = p; sm.s1 = p + nn; }
+
+    // 1. slot c <- UDT of B(beta, tau_c)^T = B_{lo}^T ... B_{L-1}^T
+    for (int c = nc - 1; c >= 0; --c) {
+        const int lo = c * se, hi = min(lo + se, L);
+        const bool first = (c == nc - 1);
+        if (first) set_identity(sm.s0, n);
+        else copy(sm.s0, slot_u(d, c + 1), nn);
+        for (int l = hi - 1; l >= lo; --l) tau_bt_left(d, sm, sm.s0, sm.s1, l, sigma);
+        udt_absorb(d, sm, sm.s0, sm.s1, first ? nullptr : slot_d(d, c + 1),
+                   first ? nullptr : slot_t(d, c + 1), slot_u(d, c), slot_d(d, c), slot_t(d, c));
+    }
+    // 2. X = G(tau_l, 0), recomputed at each chunk start and propagated up inside it
+    double* acc = d.gtau + (size_t)s * L * nn;
+    int rp = 0;
+    for (int c = 0; c < nc; ++c) {
+        const int lo = c * se, hi = min(lo + se, L);
+        const int r = nc + rp;
+        green_tau_udt(d, sm, c ? slot_u(d, r) : nullptr, slot_d(d, r), slot_t(d, r), slot_u(d, c),
+                      slot_d(d, c), slot_t(d, c), x, &singular);
+        for (int l = lo; l < hi; ++l) {
+            for (int e = threadIdx.x; e < nn; e += kNT) acc[(size_t)l * nn + e] += x[e];
+            if (l + 1 < hi) tau_b_left(d, sm, x, sm.s1, l, sigma);
+        }
+        if (c + 1 < nc) {
+            // running product B(tau_hi, 0) = B_{hi-1} ... B_lo B(tau_lo, 0)
+            const int in = nc + rp, out = nc + (rp ^ 1);
+            __syncthreads();
+            if (c == 0) set_identity(sm.s0, n);
+            else copy(sm.s0, slot_u(d, in), nn);
+            for (int l = lo; l < hi; ++l) tau_b_left(d, sm, sm.s0, sm.s1, l, sigma);
+            udt_absorb(d, sm, sm.s0, sm.s1, c ? slot_d(d, in) : nullptr,
+                       c ? slot_t(d, in) : nullptr, slot_u(d, out), slot_d(d, out), slot_t(d, out));
+            rp ^= 1;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && singular) atomicOr(d.status, LQMC_STATUS_SINGULAR);
+}
+
+// dynamic shared memory and per-chain float64 workspace (doubles) of green_tau_kernel
+size_t green_tau_smem_bytes(int n, int tau_flags) {
+    return sweep_fp64_smem_bytes(n, kGreenInGlobal | (tau_flags & kScratchInGlobal));
+}
+
+size_t green_tau_work_doubles(int n, int n_chunks, int slot, int tau_flags) {
+    const size_t nn = (size_t)n * n;
+    return 2 * ((size_t)(n_chunks + 2) * slot + nn + ((tau_flags & kScratchInGlobal) ? 2 * nn : 0));
+}
+
+cudaError_t launch_green_tau(const ChainDesc* d_descs, int n_chains, size_t smem, cudaStream_t stream) {
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(green_tau_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    green_tau_kernel<<<dim3(n_chains, 2), kNT, smem, stream>>>(d_descs);
     return cudaGetLastError();
 }
 
@@ -832,7 +1008,7 @@ extern "C" int lqmc_sweep_static(const lqmc_static_chain* c, int32_t n_sweeps, v
     e = cudaMemcpyAsync(base, &d, sizeof(d), cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) return static_fail(c, LQMC_ERR_CUDA, cudaGetErrorString(e));
     e = lqmc::launch_sweep_fp64(reinterpret_cast<const lqmc::ChainDesc*>(base), 1,
-                                lqmc::sweep_fp64_smem_bytes(n, 0), n_sweeps, c->measure ? 1 : 0, st);
+                                lqmc::sweep_fp64_smem_bytes(n, 0), n_sweeps, c->measure ? 1 : 0, 0, st);
     if (e != cudaSuccess) return static_fail(c, LQMC_ERR_CUDA, cudaGetErrorString(e));
     return LQMC_OK;
 }

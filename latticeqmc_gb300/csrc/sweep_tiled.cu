@@ -905,7 +905,8 @@ __device__ void measure_t(const ChainDesc& d, TSmem<T>& sm) {
 
 template <typename T, bool EMU>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kNT, 1)
-sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_measure) {
+sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_measure,
+                   int sweep_base) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
     extern __shared__ __align__(16) double smem[];
@@ -1037,7 +1038,8 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
         ph[k] += t_ - tc;                   \
         tc = t_;                            \
     } while (0)
-    for (int sw = 0; sw < n_sweeps; ++sw, ++sweep_id) {
+    // sw indexes the call's uniforms and decisions: sweep_base + the sweep of this launch
+    for (int sw = sweep_base; sw < sweep_base + n_sweeps; ++sw, ++sweep_id) {
         right_stack_t<T, EMU>(d, sm, sp, &logdet, &sgn, &singular);
         LQMC_PHASE(0);
         int lp = 0;
@@ -1133,23 +1135,26 @@ size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32, bool emu, int xy_d
 
 template <typename T, bool EMU>
 static cudaError_t launch_tiled(const ChainDesc* d_descs, int n_chains, size_t smem, int n_sweeps,
-                                int measure, cudaStream_t stream) {
+                                int measure, int sweep_base, cudaStream_t stream) {
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(sweep_tiled_kernel<T, EMU>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
     // two CTAs (one cluster) per chain
-    sweep_tiled_kernel<T, EMU><<<2 * n_chains, kNT, smem, stream>>>(d_descs, n_sweeps, measure);
+    sweep_tiled_kernel<T, EMU><<<2 * n_chains, kNT, smem, stream>>>(d_descs, n_sweeps, measure,
+                                                                  sweep_base);
     return cudaGetLastError();
 }
 
 // precision: 0 float64, 1 float32 (mixed), 2 float64 with emulated tensor-core GEMMs
 cudaError_t launch_sweep_tiled(const ChainDesc* d_descs, int n_chains, size_t smem, int precision,
-                               int n_sweeps, int measure, cudaStream_t stream) {
-    if (precision == 1) return launch_tiled<float, false>(d_descs, n_chains, smem, n_sweeps, measure, stream);
-    if (precision == 2) return launch_tiled<double, true>(d_descs, n_chains, smem, n_sweeps, measure, stream);
-    return launch_tiled<double, false>(d_descs, n_chains, smem, n_sweeps, measure, stream);
+                               int n_sweeps, int measure, int sweep_base, cudaStream_t stream) {
+    if (precision == 1)
+        return launch_tiled<float, false>(d_descs, n_chains, smem, n_sweeps, measure, sweep_base, stream);
+    if (precision == 2)
+        return launch_tiled<double, true>(d_descs, n_chains, smem, n_sweeps, measure, sweep_base, stream);
+    return launch_tiled<double, false>(d_descs, n_chains, smem, n_sweeps, measure, sweep_base, stream);
 }
 
 }  // namespace lqmc

@@ -86,19 +86,23 @@ class Engine:
                LQMC_FP64E_NATIVE_* mask).  Default ('lu', 'lu_rhs'): the stabilised inverse's LU
                solve in float64 (emulating its right-hand-side updates is ~5 % faster at 16x16,
                beta=8, but leaves a 7x larger median stabilisation residual)
+    measure_tau  also accumulate the unequal-time G(tau_l, 0) of every slice on each measured
+               sweep ('dqmc' only; a float64 kernel per sweep after the sweep kernel; read with
+               green_tau / green_tau_sum)
     """
 
     def __init__(self, chains, mode="dqmc", precision="fp64", rng="philox", stab_every=None,
                  delay=0, seed=0, record=False, device=0, engine="auto", debug=0,
-                 fp64e_native=("lu", "lu_rhs")):
+                 fp64e_native=("lu", "lu_rhs"), measure_tau=False):
         self.chains = list(chains)
         if stab_every is None:
             stab_every = auto_stab_every(self.chains)
         self.stab_every = int(stab_every)
         self.mode, self.precision, self.rng = mode, precision, rng
         self.record = bool(record)
+        self.measure_tau = bool(measure_tau)
         self._h = _native.Handle(mode, precision, rng, stab_every, delay, seed, record, device,
-                                 engine, debug, fp64e_native)
+                                 engine, debug, fp64e_native, measure_tau)
         n = len(self.chains)
         n_sites = np.array([c.n for c in self.chains], dtype=np.int32)
         n_slices = np.array([c.L for c in self.chains], dtype=np.int32)
@@ -177,6 +181,23 @@ class Engine:
         self._h.call("lqmc_get_green_sum", int(chain), ptr(out), ptr(cnt))
         return out, int(cnt[0])
 
+    def green_tau_sum(self, chain):
+        """Sum over the measured sweeps of G_sigma(tau_l, 0) = <c_i(tau_l) c+_j(0)>,
+        tau_l = l dtau, l = 0 .. L-1, shape (2, L, N, N), and the measurement count
+        (measure_tau=True): B(tau_l, 0) (1 + B(beta, 0))^-1 with B_l = exp_v(l) exp_k.
+        G(tau, 0) is minus lqmc.tools.compute_pole_gf_tau's G(tau) at U = 0.  The end-of-sweep
+        G that green_sum adds up is the equal-time G at tau_1: per sample
+        G(tau_1, 0) = G_sweep B_0."""
+        c = self.chains[chain]
+        out = np.empty((2, c.L, c.n, c.n))
+        self._h.call("lqmc_get_green_tau", int(chain), ptr(out))
+        return out, int(self.observables_raw(chain)[0])
+
+    def green_tau(self, chain):
+        """Mean G_sigma(tau_l, 0) over the measured sweeps, shape (2, L, N, N)."""
+        s, cnt = self.green_tau_sum(chain)
+        return s / max(cnt, 1)
+
     def observables_raw(self, chain):
         c = self.chains[chain]
         out = np.empty(_native.obs_len(c.n))
@@ -236,6 +257,8 @@ class Engine:
             arrays[f"diag_{k}"] = d
             arrays[f"gsum_{k}"] = gsum
             arrays[f"obs_{k}"] = self.observables_raw(k)
+            if self.measure_tau:
+                arrays[f"gtau_{k}"] = self.green_tau_sum(k)[0]
         np.savez(path, **arrays)
 
     def restore(self, path):
@@ -254,6 +277,11 @@ class Engine:
             g = np.ascontiguousarray(z[f"gsum_{k}"], dtype=np.float64)
             o = np.ascontiguousarray(z[f"obs_{k}"], dtype=np.float64)
             self._h.call("lqmc_set_chain_state", int(k), ptr(d), ptr(g), ptr(o))
+            if self.measure_tau:
+                if f"gtau_{k}" not in z:
+                    raise ValueError("checkpoint holds no unequal-time G sums")
+                gt = np.ascontiguousarray(z[f"gtau_{k}"], dtype=np.float64)
+                self._h.call("lqmc_set_green_tau", int(k), ptr(gt))
 
     def status(self):
         s = np.empty(len(self.chains), dtype=np.int32)

@@ -207,6 +207,21 @@ class Chain:
         return self.green
 
 
+def green_tau(exp_k, lamb, field, sigma):
+    """Unequal-time G_sigma(tau_l, 0) = B_{l-1} ... B_0 (1 + B_{L-1} ... B_0)^-1 for
+    l = 0 .. L-1, B_l = exp_v(l) exp_k (the convention of ``Chain``; the reference's get_m,
+    lqmc.py:156-185, orders its factors the same way up to the position of exp_v), from the
+    field in the reference layout (N, L).  Plain float64 products and one inverse: accurate
+    for small beta only.  Returns (L, N, N)."""
+    field = np.asarray(field)
+    n, L = field.shape
+    prods = [np.eye(n)]
+    for l in range(L):
+        prods.append(exp_v_diag(field[:, l], lamb, sigma)[:, None] * (exp_k @ prods[-1]))
+    g0 = np.linalg.inv(np.eye(n) + prods[L])
+    return np.stack([prods[l] @ g0 for l in range(L)])
+
+
 def measure(green, kinetic, u):
     """Equal-time Wick measurements from G_sigma[i, j] = <c_i c+_j> (one sample).
 

@@ -18,6 +18,7 @@ the GPU engine can be replayed against them without the reference present:
 * ``run_2x2.npz``          -- a whole ``run_lqmc()`` (``lqmc/lqmc.py:379-393``) with warm-up and
   measurement, its averaged G.
 * ``u0_known.npz``         -- the U=0 run against ``tools.compute_pole_gf_tau``
+* ``u0_gtau.npz``          -- ``tools.compute_pole_gf_tau`` at the slice times (G(tau, 0))
   (``lqmc/tools.py:193-200``).
 
 Run:  python tests/golden/make_golden.py
@@ -224,6 +225,24 @@ def u0_fixture():
     np.savez_compressed(os.path.join(HERE, "u0_known.npz"), **out)
 
 
+def u0_gtau_fixture():
+    """The reference's non-interacting imaginary-time G (tools.compute_pole_gf_tau,
+    tools.py:182-200) at the slice times tau_l = l beta / L (L divides its 2048 intervals),
+    negated to G(tau_l, 0) = <c_i(tau_l) c+_j(0)>, shape (L, N, N)."""
+    out = {}
+    for side, beta, L in ((2, 2.0, 16), (4, 8.0, 64)):
+        m = HubbardModel(u=0, t=1, mu=0)
+        m.build_square(side)
+        tau, gtau = compute_pole_gf_tau(m.ham_kinetic(), beta)
+        idx = np.arange(L) * (2048 // L)
+        assert np.allclose(tau[idx], np.arange(L) * beta / L)
+        out[f"s{side}_gtau"] = -np.moveaxis(gtau[..., idx], -1, 0)
+        out[f"s{side}_beta"] = beta
+        out[f"s{side}_L"] = L
+        out[f"s{side}_kinetic"] = m.ham_kinetic()
+    np.savez_compressed(os.path.join(HERE, "u0_gtau.npz"), **out)
+
+
 def lattice_fixtures():
     """Kinetic matrices of the reference's other lattice prefabs (lattice.py:364-421), built
     through HubbardModel with its lattice replaced: hexagonal (two-atom cell) and cubic, open
@@ -254,7 +273,7 @@ def lattice_fixtures():
 
 
 def main():
-    which = sys.argv[1:] or ["kinetic", "lattices", "compat", "det", "run", "u0"]
+    which = sys.argv[1:] or ["kinetic", "lattices", "compat", "det", "run", "u0", "u0_gtau"]
     if "kinetic" in which:
         kinetic_fixtures()
     if "lattices" in which:
@@ -270,6 +289,8 @@ def main():
         run_fixture(2, 4.0, 2.0, 20, seed=1, warmup=20, sweeps=60)
     if "u0" in which:
         u0_fixture()
+    if "u0_gtau" in which:
+        u0_gtau_fixture()
 
 
 if __name__ == "__main__":

@@ -138,6 +138,14 @@ def test_library_loads_and_exports_every_declared_symbol():
         rc = lib.lqmc_create(ctypes.byref(p), ctypes.byref(h))
         assert rc in (-1, -2)
         assert lib.lqmc_last_error(None)
+    # argument checks that come before any device call
+    import ctypes
+    p = _native.Params(mode=_native.MODES["compat"], measure_tau=1)
+    h = ctypes.c_void_p()
+    assert lib.lqmc_create(ctypes.byref(p), ctypes.byref(h)) == -4
+    assert b"dqmc" in lib.lqmc_last_error(None)
+    p = _native.Params(mode=_native.MODES["dqmc"], measure_tau=2)
+    assert lib.lqmc_create(ctypes.byref(p), ctypes.byref(h)) == -1
 
 
 def test_other_lattices_match_reference_kinetic_matrices():

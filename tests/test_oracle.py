@@ -86,6 +86,36 @@ def test_dqmc_u0_known_answer():
         assert np.abs(g[1] - f[f"s{side}_pole_tau0"]).max() < 1e-12
 
 
+def test_green_tau_oracle_u0_known_answer():
+    """The oracle's unequal-time G at U = 0 against the reference's compute_pole_gf_tau
+    (tools.py:182-200) at the slice times; beta = 2, where plain products are exact."""
+    f = golden("u0_gtau.npz")
+    K, beta, L = f["s2_kinetic"], float(f["s2_beta"]), int(f["s2_L"])
+    field = np.ones((4, L), np.int8)
+    for sigma in (1, -1):
+        g = dqmc.green_tau(expm(-beta / L * K), 0.0, field, sigma)
+        assert np.abs(g - f["s2_gtau"]).max() < 1e-13
+
+
+def test_green_tau_oracle_relations_to_equal_time_green():
+    """The end-of-sweep G of the chain (the equal-time G at tau_1) times B_0 is G(tau_1, 0),
+    and B_{L-1} G(tau_{L-1}, 0) = B(beta, 0) G(0) = 1 - G(0)."""
+    K = kinetic_from_golden(4)
+    beta, L, U = 2.0, 20, 4.0
+    dt = beta / L
+    lamb = np.arccosh(np.exp(U * dt / 2))
+    rng = np.random.default_rng(5)
+    field = (2 * rng.integers(0, 2, (16, L)) - 1).astype(np.int8)
+    ch = dqmc.Chain(expm(-dt * K), expm(dt * K), lamb, field.copy(), stab_every=5)
+    ch.sweep(np.full(16 * L, np.inf))       # u = inf rejects every flip: the field stays
+    assert (ch.field == field).all()
+    for s, sigma in ((0, 1), (1, -1)):
+        g = dqmc.green_tau(expm(-dt * K), lamb, field, sigma)
+        b = [dqmc.exp_v_diag(field[:, l], lamb, sigma)[:, None] * expm(-dt * K) for l in range(L)]
+        assert np.abs(ch.green[s] @ b[0] - g[1]).max() < 1e-11
+        assert np.abs(b[L - 1] @ g[L - 1] - (np.eye(16) - g[0])).max() < 1e-11
+
+
 def test_dqmc_stabilisation_residual_small_at_large_beta():
     K = kinetic_from_golden(8)
     beta, L, U = 10.0, 100, 4.0
