@@ -39,9 +39,10 @@ struct GemmOpt {
 };
 
 // A(i, p) = TA ? a[p * lda + i] : a[i * lda + p];  B(p, j) = TB ? b[j * ldb + p] : b[p * ldb + j]
+// Not inlined, like the emulated GEMM: one copy per (T, TA, TB) keeps the sweep kernel small.
 template <typename T, bool TA, bool TB, typename TAIn, typename TBIn>
-__device__ void tile_gemm(T* __restrict__ c, int ldc, const TAIn* a, int lda, const TBIn* b,
-                          int ldb, int m, int n, int k, T* stage, GemmOpt<T> opt = GemmOpt<T>()) {
+__device__ __noinline__ void tile_gemm(T* __restrict__ c, int ldc, const TAIn* a, int lda, const TBIn* b,
+                                       int ldb, int m, int n, int k, T* stage, GemmOpt<T> opt = GemmOpt<T>()) {
     constexpr int R = tile_r<T>();
     constexpr int D = tile_dim<T>();
     T* as = stage;                         // [kTileK][D + 1], as[p][i] = A(i0 + i, p0 + p)

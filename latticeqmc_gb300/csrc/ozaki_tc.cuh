@@ -393,8 +393,10 @@ __device__ __forceinline__ double scaled_double(long long t, int s) {
 // column scale, subtract).  A(i, p) = TA ? a[p lda + i] : a[i lda + p];
 // B(p, j) = TB ? b[j ldb + p] : b[p ldb + j].
 // pa / pb: op(A) / op(B) already split (same m, n, k); a / b are then not read.
+// Not inlined: the sweep kernel calls it from ~20 sites, and inlining each copy cost minutes
+// of compilation and pushed the kernel into register spills.
 template <bool TA, bool TB>
-__device__ void oz_gemm_tc(double* c, int ldc, const double* a, int lda, const double* b, int ldb,
+__device__ __noinline__ void oz_gemm_tc(double* c, int ldc, const double* a, int lda, const double* b, int ldb,
                            int m, int n, int k, const Workspace& ws, GemmOpt<double> opt = GemmOpt<double>(),
                            const Presplit* pa = nullptr, const Presplit* pb = nullptr) {
     Tc* tc = ws.tc;
