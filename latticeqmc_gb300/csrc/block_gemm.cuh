@@ -17,6 +17,17 @@ namespace blk {
 
 constexpr int kTileK = 16;
 
+// p, a generic pointer into the kernel's dynamic shared memory, re-derived from that array so
+// that accesses through it in a function that is not inlined compile to shared-memory
+// instructions (the compiler cannot otherwise tell where a pointer argument points)
+template <typename T>
+__device__ __forceinline__ T* as_shared(T* p) {
+    extern __shared__ __align__(16) unsigned char lqmc_dyn_smem[];
+    const int off = (int)((unsigned)__cvta_generic_to_shared(p) -
+                          (unsigned)__cvta_generic_to_shared(lqmc_dyn_smem));
+    return reinterpret_cast<T*>(lqmc_dyn_smem + off);
+}
+
 // outputs per thread along each axis: 8 x 8 in float (128 x 128 tiles, 4 FMAs per shared
 // load), 4 x 4 in double (64 x 64 tiles; the float64 pipe is the limit there)
 template <typename T>
@@ -45,6 +56,7 @@ __device__ __noinline__ void tile_gemm(T* __restrict__ c, int ldc, const TAIn* a
                                        int ldb, int m, int n, int k, T* stage, GemmOpt<T> opt = GemmOpt<T>()) {
     constexpr int R = tile_r<T>();
     constexpr int D = tile_dim<T>();
+    stage = as_shared(stage);   // the staging buffer lies in dynamic shared memory
     T* as = stage;                         // [kTileK][D + 1], as[p][i] = A(i0 + i, p0 + p)
     T* bs = stage + kTileK * (D + 1);      // [kTileK][D + 1], bs[p][j] = B(p0 + p, j0 + j)
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;

@@ -393,13 +393,16 @@ __device__ __forceinline__ double scaled_double(long long t, int s) {
 // column scale, subtract).  A(i, p) = TA ? a[p lda + i] : a[i lda + p];
 // B(p, j) = TB ? b[j ldb + p] : b[p ldb + j].
 // pa / pb: op(A) / op(B) already split (same m, n, k); a / b are then not read.
-// Not inlined: the sweep kernel calls it from ~20 sites, and inlining each copy cost minutes
-// of compilation and pushed the kernel into register spills.
+// oz_gemm_tc_impl is the body, inlined where the caller asks for it (the most frequent
+// products); oz_gemm_tc, below, is one out-of-line copy per (TA, TB) for every other call
+// site: inlining all ~20 of them cost minutes of compilation and spilled registers.
 template <bool TA, bool TB>
-__device__ __noinline__ void oz_gemm_tc(double* c, int ldc, const double* a, int lda, const double* b, int ldb,
-                           int m, int n, int k, const Workspace& ws, GemmOpt<double> opt = GemmOpt<double>(),
-                           const Presplit* pa = nullptr, const Presplit* pb = nullptr) {
+__device__ __forceinline__ void oz_gemm_tc_impl(double* c, int ldc, const double* a, int lda,
+                                                const double* b, int ldb, int m, int n, int k,
+                                                const Workspace ws, GemmOpt<double> opt,
+                                                const Presplit* pa, const Presplit* pb) {
     Tc* tc = ws.tc;
+    unsigned char* const stage = as_shared(ws.stage);
     // callers may have just written A or B; order earlier generic shared-memory use of the
     // stage before the asynchronous copies into it
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
@@ -418,7 +421,7 @@ __device__ __noinline__ void oz_gemm_tc(double* c, int ldc, const double* a, int
     const int* ea = pa ? pa->exps : ws.ea;
     const int* eb = pb ? pb->exps : ws.eb;
     const long long t0 = clock64();
-    int* scratch = reinterpret_cast<int*>(ws.stage);   // the stage is idle while splitting
+    int* scratch = reinterpret_cast<int*>(stage);   // the stage is idle while splitting
     const int* ksa = nullptr;
     const int* ksb = nullptr;
     if (opt.kscale && !pa && !pb && k <= kMaxKscale) {
@@ -465,7 +468,7 @@ __device__ __noinline__ void oz_gemm_tc(double* c, int ldc, const double* a, int
             if (threadIdx.x == 0 && !failed) {
                 uint32_t ph = tc->phase;
                 auto load = [&](int s, int buf) {
-                    unsigned char* st = ws.stage + (size_t)buf * (kStepA + kStepB) * 2;
+                    unsigned char* st = stage + (size_t)buf * (kStepA + kStepB) * 2;
                     expect_tx(&tc->bar[buf], (kStepA + kStepB) * 2);
                     bulk_load(st, sa + (size_t)(tm * S + s0 + s) * kStepA, kStepA * 2, &tc->bar[buf]);
                     bulk_load(st + kStepA * 2, sb + (size_t)(tn * S + s0 + s) * kStepB, kStepB * 2, &tc->bar[buf]);
@@ -481,7 +484,7 @@ __device__ __noinline__ void oz_gemm_tc(double* c, int ldc, const double* a, int
                     const int buf = s % stages;
                     if (!wait(buf)) { failed = true; break; }
                     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                    const uint32_t st = smem_u32(ws.stage + (size_t)buf * (kStepA + kStepB) * 2);
+                    const uint32_t st = smem_u32(stage + (size_t)buf * (kStepA + kStepB) * 2);
                     // A_t times the stacked B_0 .. B_{7-t}: the accumulators of diagonals
                     // t .. 7 are the contiguous TMEM columns [64 t, 512), so one MMA of
                     // N = 64 (8 - t) (cut at 256) covers every pair of this t
@@ -519,7 +522,7 @@ __device__ __noinline__ void oz_gemm_tc(double* c, int ldc, const double* a, int
             // epilogue, in two halves of 32 columns: each thread combines 16 outputs of its
             // row (two groups of 8 columns, all 8 diagonals read before one wait), the half is
             // transposed through the stage buffer, and written with whole-row coalesced stores
-            double* ts = reinterpret_cast<double*>(ws.stage);   // [kBM][kTs]
+            double* ts = reinterpret_cast<double*>(stage);   // [kBM][kTs]
             constexpr int kTs = 33;
             const int ei = (i0 + row < m) ? ea[i0 + row] : 0;
             // |D_d| <= 8 k 64^2 < 2^22 for the k of this chunk
@@ -606,6 +609,14 @@ __device__ __noinline__ void oz_gemm_tc(double* c, int ldc, const double* a, int
         }
     }
     if (ws.cycles && threadIdx.x == 0) ws.cycles[1] += clock64() - t1;
+}
+
+template <bool TA, bool TB>
+__device__ __noinline__ void oz_gemm_tc(double* c, int ldc, const double* a, int lda, const double* b,
+                                        int ldb, int m, int n, int k, const Workspace ws,
+                                        GemmOpt<double> opt = GemmOpt<double>(),
+                                        const Presplit* pa = nullptr, const Presplit* pb = nullptr) {
+    oz_gemm_tc_impl<TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, ws, opt, pa, pb);
 }
 
 }  // namespace ozt

@@ -120,6 +120,14 @@ template <typename T> __device__ __forceinline__ double* slot_d(const TSmem<T>& 
     return reinterpret_cast<double*>(slot_U(sm, idx, nn) + 2 * nn);
 }
 
+// Product categories whose emulated GEMMs are inlined at their call sites: the most frequent
+// ones (the per-slice wraps and the delayed-update flushes, four call sites); every other
+// site calls the single out-of-line copy.
+#ifndef LQMC_OZ_INLINE_CATS
+#define LQMC_OZ_INLINE_CATS (LQMC_FP64E_NATIVE_WRAP | LQMC_FP64E_NATIVE_UPDATE)
+#endif
+constexpr int kInlineCats = LQMC_OZ_INLINE_CATS;
+
 // Dense product of the tiled kernel: the block-tiled SIMT GEMM, or with EMU the float64
 // GEMM emulated on the tcgen05 BF16 tensor cores (ozaki_tc.cuh), unless the product's
 // category (LQMC_FP64E_NATIVE_* bit) is kept in native float64 for this chain.
@@ -129,6 +137,9 @@ __device__ __forceinline__ void gemm_t(TSmem<T>& sm, T* c, int ldc, const TAIn* 
                                        GemmOpt<T> o = GemmOpt<T>(), int pa = -1, int pb = -1) {
     if constexpr (EMU) {
         if (sm.native & Cat) tile_gemm<T, TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.stage64, o);
+        else if constexpr ((Cat & kInlineCats) != 0)
+            ozt::oz_gemm_tc_impl<TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.oz, o,
+                                         pa >= 0 ? &sm.pre[pa] : nullptr, pb >= 0 ? &sm.pre[pb] : nullptr);
         else ozt::oz_gemm_tc<TA, TB>(c, ldc, a, lda, b, ldb, m, n, k, sm.oz, o,
                                      pa >= 0 ? &sm.pre[pa] : nullptr, pb >= 0 ? &sm.pre[pb] : nullptr);
     } else {

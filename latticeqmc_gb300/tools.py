@@ -1,5 +1,22 @@
 """Post-processing helpers with the reference's names and semantics (lqmc/tools.py)."""
+import os
+
 import numpy as np
+
+
+def get_datapath(filename, model, post='', mkdir=True, **kwargs):
+    """Result-file path of a model and run parameters (lqmc/tools.py:12-38).
+
+    The folder is data/u=<u>_t=<t>_mu=<mu>_w=<width>_h=<height> below the working
+    directory (created when mkdir), the file "<filename> <k1=v1_k2=v2...><post>.npz"; the
+    absolute path is returned.
+    """
+    width, height = model.lattice.shape
+    folder = os.path.join("data", f"u={model.u}_t={model.t}_mu={model.mu}_w={width}_h={height}")
+    if mkdir:
+        os.makedirs(folder, exist_ok=True)
+    params = "_".join(f"{key}={val}" for key, val in kwargs.items())
+    return os.path.abspath(os.path.join(folder, f"{filename} {params}{post}.npz"))
 
 
 def check_params(u, t, dtau):

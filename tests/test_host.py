@@ -107,6 +107,16 @@ def test_tools_match_reference_semantics():
     assert abs(tools.fermi_fct(0.0, 3.0) - 0.5) < 1e-15
 
 
+def test_get_datapath_like_reference(tmp_path, monkeypatch):
+    monkeypatch.chdir(tmp_path)
+    m = HubbardModel(u=4, t=1, mu=0)
+    m.build_square(4)
+    p = tools.get_datapath("gf", m, post="_tmp", beta=2, L=20)
+    folder = tmp_path / "data" / "u=4_t=1_mu=0_w=4_h=4"
+    assert p == str(folder / "gf beta=2_L=20_tmp.npz")
+    assert folder.is_dir()
+
+
 def _header_symbols():
     with open(os.path.join(ROOT, "include", "lqmc_gpu.h")) as fh:
         text = fh.read()
