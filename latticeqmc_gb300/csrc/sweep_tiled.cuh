@@ -121,10 +121,10 @@ template <typename T> __device__ __forceinline__ double* slot_d(const TSmem<T>& 
 }
 
 // Product categories whose emulated GEMMs are inlined at their call sites: the most frequent
-// ones (the per-slice wraps and the delayed-update flushes, four call sites); every other
-// site calls the single out-of-line copy.
+// ones (the per-slice wraps, the delayed-update flushes and the B-chain products, seven call
+// sites); every other site calls the single out-of-line copy.
 #ifndef LQMC_OZ_INLINE_CATS
-#define LQMC_OZ_INLINE_CATS (LQMC_FP64E_NATIVE_WRAP | LQMC_FP64E_NATIVE_UPDATE)
+#define LQMC_OZ_INLINE_CATS (LQMC_FP64E_NATIVE_WRAP | LQMC_FP64E_NATIVE_UPDATE | LQMC_FP64E_NATIVE_STACK)
 #endif
 constexpr int kInlineCats = LQMC_OZ_INLINE_CATS;
 
