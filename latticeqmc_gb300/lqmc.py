@@ -11,7 +11,13 @@ rng         'replay' (default): one ``np.random.rand()`` per site from numpy's g
             generator, in sweep order, exactly as lqmc.py:317 draws them.  'philox': on device.
 stab_every  slices between from-scratch refreshes of G (dqmc); default: the largest with
             stab_every * dtau <= 0.5.
-precision   'fp64'.
+precision   'fp64' (default); 'fp64e' (float64 G, every dense product a float64-accurate
+            GEMM emulated on the tensor cores; dqmc mode); 'mixed' (float32, dqmc mode).
+delay       delayed-update depth of the tiled kernel (0: automatic).
+engine      'auto', 'smem' or 'tiled' (see Engine).
+fp64e_native  product categories the fp64e engine keeps in native float64 (see Engine).
+measure_tau also accumulate the unequal-time G(tau_l, 0) on every measured sweep (dqmc mode;
+            read with green_tau()).
 
 ``det_mode=True`` runs the exact-ratio chain (mode 'dqmc'): its ratios equal the reference's
 determinant ratios (lqmc.py:244-248) to rounding.
@@ -35,7 +41,8 @@ class LatticeQMC:
 
     def __init__(self, model, beta, time_steps, warmup=300, sweeps=2000, det_mode=False,
                  log_lvl=DEBUG, *, mode=None, precision="fp64", rng=None, stab_every=None,
-                 seed=0, device=0):
+                 seed=0, device=0, delay=0, engine="auto", fp64e_native=("lu", "lu_rhs"),
+                 measure_tau=False):
         self.logger = _log if log_lvl is not None else None
         if self.logger is not None:
             self.logger.setLevel(log_lvl)
@@ -52,6 +59,10 @@ class LatticeQMC:
         self.stab_every = stab_every
         self.seed = seed
         self.device = device
+        self.delay = delay
+        self.engine_kind = engine
+        self.fp64e_native = fp64e_native
+        self.measure_tau = bool(measure_tau)
         self.status = ""
         self.it = 0
         self.ratio = 0.0
@@ -88,7 +99,8 @@ class LatticeQMC:
         if self._engine is None:
             self._engine = Engine([self._spec], mode=self.mode, precision=self.precision,
                                   rng=self.rng, stab_every=self.stab_every, seed=self.seed,
-                                  device=self.device)
+                                  device=self.device, delay=self.delay, engine=self.engine_kind,
+                                  fp64e_native=self.fp64e_native, measure_tau=self.measure_tau)
         return self._engine
 
     # -- sweeps ----------------------------------------------------------------------------
@@ -127,6 +139,14 @@ class LatticeQMC:
     def observables(self):
         """Wick observables averaged over the last measurement loop."""
         return self.engine.observables(0)
+
+    def green_tau(self):
+        """Mean unequal-time G_sigma(tau_l, 0), l = 0 .. L-1, over the last measurement loop,
+        shape (2, L, N, N) (measure_tau=True); minus lqmc.tools.compute_pole_gf_tau's G(tau)
+        at U = 0."""
+        if not self.measure_tau:
+            raise ValueError("green_tau needs LatticeQMC(..., measure_tau=True)")
+        return self.engine.green_tau(0)
 
     def run_lqmc(self):
         self.warmup_loop()

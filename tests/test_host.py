@@ -191,3 +191,28 @@ def test_periodic_hexagonal_and_cubic_lattices():
     m.lattice = Lattice.cubic()
     m.build(3, 3, None)
     assert m.n_sites == 9
+
+
+def test_lattice_qmc_forwards_engine_options(monkeypatch):
+    import latticeqmc_gb300.lqmc as lqmc_mod
+    seen = {}
+
+    class StandIn:
+        def __init__(self, chains, **kw):
+            seen.update(kw, n_chains=len(chains))
+
+    monkeypatch.setattr(lqmc_mod, "Engine", StandIn)
+    m = HubbardModel(u=4, t=1, mu=0)
+    m.build_square(4)
+    np.random.seed(0)
+    s = lqmc_mod.LatticeQMC(m, 2.0, 20, log_lvl=None, mode="dqmc", precision="fp64e", rng="philox",
+                            stab_every=5, seed=7, delay=12, engine="tiled", fp64e_native=("lu",),
+                            measure_tau=True)
+    s.engine
+    assert seen == dict(n_chains=1, mode="dqmc", precision="fp64e", rng="philox", stab_every=5,
+                        seed=7, device=0, delay=12, engine="tiled", fp64e_native=("lu",),
+                        measure_tau=True)
+    plain = lqmc_mod.LatticeQMC(m, 2.0, 20, log_lvl=None)
+    assert plain.mode == "compat" and plain.rng == "replay"
+    with pytest.raises(ValueError):
+        plain.green_tau()
