@@ -3,7 +3,8 @@
 Each CUDA translation unit under ``csrc/`` is compiled in parallel to an object file in
 ``_build/`` and linked into ``latticeqmc_gb300/liblqmc_gpu.so`` (static cudart, so the
 library loads without a CUDA toolkit on the library path).  Objects are rebuilt only when a
-source or header is newer than them.
+source or header is newer than them, or when the extra nvcc flags differ from those they
+were compiled with (``python -m latticeqmc_gb300.build -DNAME=VALUE ...``).
 
     python -m latticeqmc_gb300.build
 """
@@ -52,13 +53,21 @@ def build(verbose=False, extra=()):
     os.makedirs(BUILD, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     hdr_t = _newest_header()
+    # the objects were compiled with these extra flags; any change rebuilds everything
+    stamp = os.path.join(BUILD, "extra_flags.txt")
+    flags = " ".join(extra)
+    try:
+        with open(stamp) as fh:
+            same_flags = fh.read() == flags
+    except OSError:
+        same_flags = not flags
     jobs = []
     objs = []
     for src in srcs:
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
         objs.append(obj)
         if (not os.path.exists(obj) or os.path.getmtime(obj) < max(os.path.getmtime(src), hdr_t)
-                or extra):
+                or not same_flags):
             jobs.append((src, obj))
     if jobs:
         with concurrent.futures.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
@@ -67,6 +76,8 @@ def build(verbose=False, extra=()):
                 msg = f.result()
                 if verbose and msg.strip():
                     print(msg, file=sys.stderr)
+        with open(stamp, "w") as fh:
+            fh.write(flags)
     if jobs or not os.path.exists(LIB):
         tmp = LIB + ".tmp"
         cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-cudart", "static"]
