@@ -20,6 +20,8 @@ the GPU engine can be replayed against them without the reference present:
 * ``u0_known.npz``         -- the U=0 run against ``tools.compute_pole_gf_tau``
 * ``u0_gtau.npz``          -- ``tools.compute_pole_gf_tau`` at the slice times (G(tau, 0))
   (``lqmc/tools.py:193-200``).
+* ``exact_chain10_gtau.npz`` -- the reference's own U=0 check (``exact.py:37-54``): a 10-site
+  open chain at beta = 4, ``compute_pole_gf_tau`` at the slice times.
 
 Run:  python tests/golden/make_golden.py
 """
@@ -243,6 +245,21 @@ def u0_gtau_fixture():
     np.savez_compressed(os.path.join(HERE, "u0_gtau.npz"), **out)
 
 
+def exact_chain_fixture():
+    """exact.py:37-54 of the reference: U = 0, t = 1, mu = U/2, a 10-site chain built with
+    open boundaries (``build(n_sites, cycling=None)``), beta = 4; its non-interacting G(tau)
+    from tools.compute_pole_gf_tau, negated to G(tau_l, 0) at tau_l = l beta / L, L = 32."""
+    n_sites, u, t, beta, L = 10, 0, 1, 4.0, 32
+    m = HubbardModel(u=u, t=t, mu=u / 2)
+    m.build(n_sites, cycling=None)
+    ham = m.ham_kinetic()
+    tau, gtau = compute_pole_gf_tau(ham, beta)
+    idx = np.arange(L) * (2048 // L)
+    assert np.allclose(tau[idx], np.arange(L) * beta / L)
+    np.savez_compressed(os.path.join(HERE, "exact_chain10_gtau.npz"), kinetic=ham, beta=beta, L=L,
+                        gtau=-np.moveaxis(gtau[..., idx], -1, 0))
+
+
 def lattice_fixtures():
     """Kinetic matrices of the reference's other lattice prefabs (lattice.py:364-421), built
     through HubbardModel with its lattice replaced: hexagonal (two-atom cell) and cubic, open
@@ -273,7 +290,8 @@ def lattice_fixtures():
 
 
 def main():
-    which = sys.argv[1:] or ["kinetic", "lattices", "compat", "det", "run", "u0", "u0_gtau"]
+    which = sys.argv[1:] or ["kinetic", "lattices", "compat", "det", "run", "u0", "u0_gtau",
+                             "exact_chain"]
     if "kinetic" in which:
         kinetic_fixtures()
     if "lattices" in which:
@@ -291,6 +309,8 @@ def main():
         u0_fixture()
     if "u0_gtau" in which:
         u0_gtau_fixture()
+    if "exact_chain" in which:
+        exact_chain_fixture()
 
 
 if __name__ == "__main__":

@@ -216,3 +216,10 @@ def test_lattice_qmc_forwards_engine_options(monkeypatch):
     assert plain.mode == "compat" and plain.rng == "replay"
     with pytest.raises(ValueError):
         plain.green_tau()
+
+
+def test_open_chain_kinetic_matches_reference_exact_script():
+    """exact.py:43-45 of the reference builds a 10-site chain with open boundaries."""
+    m = HubbardModel(u=0, t=1, mu=0)
+    m.build(10, cycling=None)
+    np.testing.assert_array_equal(m.ham_kinetic(), golden("exact_chain10_gtau.npz")["kinetic"])

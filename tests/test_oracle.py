@@ -185,3 +185,14 @@ def test_philox_uniforms_in_unit_interval_and_distinct_streams():
     assert a.min() >= 0.0 and a.max() < 1.0
     assert not np.array_equal(a, b) and not np.array_equal(a, c)
     assert abs(np.concatenate([a, b, c]).mean() - 0.5) < 0.05
+
+
+def test_green_tau_oracle_matches_reference_exact_chain():
+    """The reference's own U = 0 validation (exact.py:37-54): a 10-site open chain at beta = 4,
+    G(tau_l, 0) against its compute_pole_gf_tau at the 32 slice times."""
+    f = golden("exact_chain10_gtau.npz")
+    K, beta, L = f["kinetic"], float(f["beta"]), int(f["L"])
+    field = np.ones((K.shape[0], L), np.int8)
+    for sigma in (1, -1):
+        g = dqmc.green_tau(expm(-beta / L * K), 0.0, field, sigma)
+        assert np.abs(g - f["gtau"]).max() < 1e-12
