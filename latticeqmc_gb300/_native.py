@@ -100,6 +100,15 @@ def ptr(a):
     return a.ctypes.data_as(ctypes.c_void_p)
 
 
+def _choice(table, value, what):
+    """table[value], or ValueError naming the accepted values (the reference raises ValueError
+    for bad arguments, lqmc/multiprocessing.py:108)."""
+    try:
+        return table[value]
+    except (KeyError, TypeError):
+        raise ValueError(f"unknown {what} {value!r}; expected one of {sorted(table)}") from None
+
+
 class Handle:
     """Owns one lqmc_handle; every call checks the return code."""
 
@@ -114,9 +123,12 @@ class Handle:
                 if name not in FP64E_NATIVE:
                     raise ValueError(f"unknown fp64e product category {name!r}")
                 native |= FP64E_NATIVE[name]
-        p = Params(mode=MODES[mode], precision=PRECISIONS[precision], rng=RNGS[rng],
+        p = Params(mode=_choice(MODES, mode, "mode"),
+                   precision=_choice(PRECISIONS, precision, "precision"),
+                   rng=_choice(RNGS, rng, "rng"),
                    stab_every=int(stab_every), delay=int(delay), record=int(bool(record)),
-                   seed=int(seed) & ((1 << 64) - 1), device=int(device), engine=ENGINES[engine],
+                   seed=int(seed) & ((1 << 64) - 1), device=int(device),
+                   engine=_choice(ENGINES, engine, "engine"),
                    debug=int(debug), fp64e_native=int(native),
                    measure_tau=int(bool(measure_tau)))
         h = ctypes.c_void_p()

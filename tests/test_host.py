@@ -223,3 +223,13 @@ def test_open_chain_kinetic_matches_reference_exact_script():
     m = HubbardModel(u=0, t=1, mu=0)
     m.build(10, cycling=None)
     np.testing.assert_array_equal(m.ham_kinetic(), golden("exact_chain10_gtau.npz")["kinetic"])
+
+
+@pytest.mark.parametrize("kw", [dict(mode="fast"), dict(precision="fp16"), dict(rng="mt19937"),
+                                dict(engine="cluster"), dict(fp64e_native=("wraps",))])
+def test_bad_engine_names_raise_value_error_before_any_device_call(kw):
+    args = dict(mode="dqmc", precision="fp64", rng="philox", stab_every=5, delay=0, seed=0,
+                record=False, device=0)
+    args.update(kw)
+    with pytest.raises(ValueError):
+        _native.Handle(**args)
