@@ -21,6 +21,9 @@ measure_tau also accumulate the unequal-time G(tau_l, 0) on every measured sweep
 
 ``det_mode=True`` runs the exact-ratio chain (mode 'dqmc'): its ratios equal the reference's
 determinant ratios (lqmc.py:244-248) to rounding.
+The reference's determinant mode itself (every ratio from det M of the flipped field,
+lqmc.py:236-299) runs on the device through ``warmup_loop_det``, ``measure_loop_det`` and
+``_update_step_det`` (engine mode 'det'; small lattices).
 """
 import logging
 import time
@@ -73,6 +76,7 @@ class LatticeQMC:
         self.lamb = 0.
         self.exp_k = None
         self._engine = None
+        self._engine_det = None
         self._log_info(f"Warmup=     {self.warm_sweeps}")
         self._log_info(f"Measurement={self.meas_sweeps}")
         self.set_beta(beta)
@@ -87,6 +91,7 @@ class LatticeQMC:
         self.beta = beta
         self.lamb = hs_coupling(self.model.u, self.dtau)
         self._engine = None
+        self._engine_det = None
         spec = ChainSpec(self.ham_kin, self.model.u, beta, self.time_steps, self.config.config)
         self.exp_k = spec.exp_k
         self._spec = spec
@@ -103,9 +108,30 @@ class LatticeQMC:
                                   fp64e_native=self.fp64e_native, measure_tau=self.measure_tau)
         return self._engine
 
+    def _det_engine(self):
+        """The device engine of the reference's determinant mode (mode 'det', float64)."""
+        if self._engine_det is None:
+            self._engine_det = Engine([self._spec], mode="det", precision="fp64", rng=self.rng,
+                                      stab_every=self.stab_every, seed=self.seed,
+                                      device=self.device)
+        return self._engine_det
+
+    def iter_sweeps(self, n, console_updates=200):
+        """Yield 0 .. n-1 with ``self.it`` set and a progress line on the console every
+        n / console_updates sweeps, as lqmc.py:187-215."""
+        every = max(1, int(n / console_updates))
+        for it in range(n):
+            if (it + 1) % every == 0:
+                print(f"\r{self.status} Sweep {it + 1} ({100 * (it + 1) / n:.1f}%) "
+                      f"[Mean: {self.config.mean():5.2f}, Var: {self.config.var():5.2f}]",
+                      end="", flush=True)
+            self.it = it
+            yield it
+        print(f"\r{self.status} Sweep {n} (100.0%)")
+
     # -- sweeps ----------------------------------------------------------------------------
-    def _run(self, n_sweeps, measure):
-        eng = self.engine
+    def _run(self, n_sweeps, measure, eng=None):
+        eng = eng if eng is not None else self.engine
         eng.set_field(0, self.config.config)
         per = self.n_sites * self.time_steps
         done = 0
@@ -134,6 +160,34 @@ class LatticeQMC:
         self.engine.reset_measurements()
         self._run(self.meas_sweeps, True)
         gsum, cnt = self.engine.green_sum(0)
+        return gsum / max(cnt, 1)
+
+    # -- the reference's determinant mode (lqmc.py:236-299), on the device ---------------------
+    def _update_step_det(self, old_det=None):
+        """One determinant-mode sweep (lqmc.py:236-259): every flip's ratio is
+        det M_up det M_dn of the flipped field over the current one.  Returns that product for
+        the field the sweep leaves, as the reference returns its running old_det (which is
+        always a fresh determinant).  ``old_det`` is taken for the reference's signature; the
+        device computes it from the field."""
+        eng = self._det_engine()
+        self._run(1, False, eng)
+        d = eng.diagnostics(0)
+        # the kernel keeps log|det G_sigma| = -log|det M_sigma| and sign(det M_sigma)
+        return float(np.prod(d["sign"]) * np.exp(-np.sum(d["logdet"])))
+
+    def warmup_loop_det(self):
+        """Warm-up sweeps of the determinant mode (lqmc.py:261-271)."""
+        self.status = "Warmup"
+        self._run(self.warm_sweeps, False, self._det_engine())
+
+    def measure_loop_det(self):
+        """Mean of inv(get_m(0, sigma)) over the determinant-mode measurement sweeps
+        (lqmc.py:273-299)."""
+        self.status = "Measurement"
+        eng = self._det_engine()
+        eng.reset_measurements()
+        self._run(self.meas_sweeps, True, eng)
+        gsum, cnt = eng.green_sum(0)
         return gsum / max(cnt, 1)
 
     def observables(self):

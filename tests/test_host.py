@@ -233,3 +233,57 @@ def test_bad_engine_names_raise_value_error_before_any_device_call(kw):
     args.update(kw)
     with pytest.raises(ValueError):
         _native.Handle(**args)
+
+
+def test_lattice_qmc_determinant_mode_loops_drive_a_det_engine(monkeypatch):
+    import latticeqmc_gb300.lqmc as lqmc_mod
+    made = []
+
+    class StandIn:
+        def __init__(self, chains, mode, **kw):
+            self.mode, self.kw, self.sweeps, self.measured = mode, kw, [], 0
+            self.f = chains[0].field.copy()
+            made.append(self)
+
+        def set_field(self, c, f):
+            self.f = np.array(f, copy=True)
+
+        def field(self, c):
+            return self.f.copy()
+
+        def set_uniforms(self, c, u):
+            assert u.size % self.f.size == 0
+
+        def sweep(self, k, measure=False):
+            self.sweeps.append((k, measure))
+            self.f[0, 0] *= -1
+            self.measured += k if measure else 0
+
+        def reset_measurements(self):
+            self.measured = 0
+
+        def green_sum(self, c):
+            n = self.f.shape[0]
+            return np.full((2, n, n), 3.0 * self.measured), self.measured
+
+        def diagnostics(self, c):
+            return {"logdet": np.array([-1.5, -0.5]), "sign": np.array([1.0, -1.0])}
+
+    monkeypatch.setattr(lqmc_mod, "Engine", StandIn)
+    m = HubbardModel(u=4, t=1, mu=0)
+    m.build_square(2)
+    np.random.seed(3)
+    s = lqmc_mod.LatticeQMC(m, 2.0, 20, warmup=4, sweeps=6, log_lvl=None)
+    f0 = s.config.config.copy()
+    s.warmup_loop_det()
+    eng = made[-1]
+    assert eng.mode == "det" and eng.kw["precision"] == "fp64"
+    assert sum(k for k, meas in eng.sweeps if not meas) == 4
+    assert s.config.config[0, 0] == f0[0, 0] * (-1) ** len(eng.sweeps)
+    gf = s.measure_loop_det()
+    np.testing.assert_array_equal(gf, np.full((2, 4, 4), 3.0))
+    assert abs(s._update_step_det(123.0) - (-np.exp(2.0))) < 1e-12
+    assert len(made) == 1                    # one det engine, reused
+    s.set_beta(1.0)
+    s.warmup_loop_det()
+    assert len(made) == 2                    # a new beta rebuilds it
