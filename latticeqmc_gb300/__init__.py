@@ -15,13 +15,17 @@ from .engine import ChainSpec, Engine
 from .hubbard import HubbardModel
 from .lattice import Lattice
 from .lqmc import LatticeQMC
+from .managers import ParallelProcessManager, SerialProcessManager
 from .scans import scan
-from .tools import (check_params, compute_pole_gf_tau, fermi_fct, filling, local_gf,
-                    local_moment, matsubara_frequencies, pole_gf_tau)
+from .tools import (check_params, compute_pole_gf_tau, decompose, fermi_fct, filling,
+                    get_datapath, local_gf, local_moment, matsubara_frequencies, pole_gf_tau,
+                    reconstruct)
 
 __all__ = ["Configuration", "ChainSpec", "Engine", "HubbardModel", "Lattice", "LatticeQMC",
-           "measure", "measure_betas", "scan", "check_params", "compute_pole_gf_tau", "fermi_fct",
-           "filling", "local_gf", "local_moment", "matsubara_frequencies", "pole_gf_tau"]
+           "ParallelProcessManager", "SerialProcessManager", "measure", "measure_betas", "scan",
+           "check_params", "compute_pole_gf_tau", "decompose", "fermi_fct", "filling",
+           "get_datapath", "local_gf", "local_moment", "matsubara_frequencies", "pole_gf_tau",
+           "reconstruct"]
 
 _DEFAULT_CHAINS = 16
 

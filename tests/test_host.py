@@ -287,3 +287,39 @@ def test_lattice_qmc_determinant_mode_loops_drive_a_det_engine(monkeypatch):
     s.set_beta(1.0)
     s.warmup_loop_det()
     assert len(made) == 2                    # a new beta rebuilds it
+
+
+def test_process_managers_drive_the_batched_entry_points(monkeypatch):
+    import latticeqmc_gb300 as pkg
+    calls = []
+
+    def fake_measure(model, beta, time_steps, warmup, sweeps, cores=None, det_mode=False, **kw):
+        calls.append(("measure", beta, time_steps, warmup, sweeps, cores, det_mode, kw))
+        n = model.n_sites
+        return np.full((n, n), 1.0), np.full((n, n), 2.0)
+
+    def fake_measure_betas(model, betas, time_steps, warmup=500, sweeps=5000, cores=-1,
+                           caching=True, det_mode=False, **kw):
+        calls.append(("measure_betas", list(betas), time_steps, warmup, sweeps, caching, det_mode))
+        n, m = model.n_sites, len(betas)
+        return np.zeros((m, n, n)), np.ones((m, n, n))
+
+    monkeypatch.setattr(pkg, "measure", fake_measure)
+    monkeypatch.setattr(pkg, "measure_betas", fake_measure_betas)
+    model = HubbardModel(u=4, t=1, mu=0)
+    model.build_square(2)
+    # as lqmc/__init__.py:17-55 uses it
+    mgr = pkg.ParallelProcessManager(model, 2.0, 20, 30, False, procs=8, mode="dqmc")
+    mgr.set_jobs(1000)
+    mgr.run()
+    gf = mgr.get_result()
+    mgr.terminate()
+    assert gf.shape == (2, 4, 4) and gf[0, 0, 0] == 1.0 and gf[1, 0, 0] == 2.0
+    assert calls[-1] == ("measure", 2.0, 20, 30, 1000, 8, False, {"mode": "dqmc"})
+    # as lqmc/__init__.py:57-96 uses it
+    mgr = pkg.SerialProcessManager(model, 20, 50, 400, False, -1, False)
+    mgr.set_jobs([1.0, 2.0, 4.0])
+    mgr.run(sleep=1.0)
+    gf_up, gf_dn = np.swapaxes(mgr.get_result(), 0, 1)
+    assert gf_up.shape == (3, 4, 4) and (gf_up == 0).all() and (gf_dn == 1).all()
+    assert calls[-1] == ("measure_betas", [1.0, 2.0, 4.0], 20, 50, 400, False, False)
