@@ -323,3 +323,20 @@ def test_process_managers_drive_the_batched_entry_points(monkeypatch):
     gf_up, gf_dn = np.swapaxes(mgr.get_result(), 0, 1)
     assert gf_up.shape == (3, 4, 4) and (gf_up == 0).all() and (gf_dn == 1).all()
     assert calls[-1] == ("measure_betas", [1.0, 2.0, 4.0], 20, 50, 400, False, False)
+
+
+def test_bench_algorithmic_work_matches_the_worked_example():
+    """Flops of one sweep of a 16x16 chain (N = 256, L = 80) at acceptance 0.5 with a
+    refresh every 10 slices: wraps 8 L N^3, B-chain 4 L N^3, QR 2 (L / n_s) (4/3) N^3,
+    updates 4 A N^2 (A accepted flips) = 1.07e10 + 5.4e9 + 3.6e8 + 2.7e9."""
+    import sys
+    import types
+    if ROOT not in sys.path:
+        sys.path.insert(0, ROOT)
+    import bench
+    n, L = 256, 80
+    spec = types.SimpleNamespace(n=n, L=L)
+    flops = bench.algorithmic_flops([spec], [0.5 * n * L], 10)
+    parts = 8 * L * n ** 3 + 4 * L * n ** 3 + 2 * 8 * (4 / 3) * n ** 3 + 4 * 0.5 * n * L * n ** 2
+    assert flops == pytest.approx(parts, rel=1e-12)
+    assert flops == pytest.approx(1.07e10 + 5.37e9 + 3.58e8 + 2.68e9, rel=5e-3)
