@@ -340,3 +340,21 @@ def test_bench_algorithmic_work_matches_the_worked_example():
     parts = 8 * L * n ** 3 + 4 * L * n ** 3 + 2 * 8 * (4 / 3) * n ** 3 + 4 * 0.5 * n * L * n ** 2
     assert flops == pytest.approx(parts, rel=1e-12)
     assert flops == pytest.approx(1.07e10 + 5.37e9 + 3.58e8 + 2.68e9, rel=5e-3)
+
+
+def test_documented_c_caller_compiles_against_the_header(tmp_path):
+    """The minimal C caller of the integration guide compiles against include/lqmc_gpu.h."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no C compiler")
+    with open(os.path.join(ROOT, "INTEGRATION.md")) as fh:
+        blocks = re.findall(r"```c\n(.*?)```", fh.read(), re.S)
+    assert blocks, "no C example in the integration guide"
+    src = tmp_path / "caller.c"
+    src.write_text(blocks[0])
+    r = subprocess.run([gcc, "-std=c11", "-Wall", "-Wextra", "-Werror", "-I",
+                        os.path.join(ROOT, "include"), "-c", str(src), "-o",
+                        str(tmp_path / "caller.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
