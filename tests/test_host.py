@@ -360,30 +360,47 @@ def test_documented_c_caller_compiles_against_the_header(tmp_path):
     assert r.returncode == 0, r.stderr
 
 
-def test_ctypes_params_layout_matches_the_c_struct(tmp_path):
-    """Every field of the binding's lqmc_params (and of the guide's stub) sits at the C
-    compiler's offset, and the sizes agree."""
-    import ctypes
+def _c_layout(tmp_path, struct, fields):
+    """sizeof(struct) and offsetof(struct, f) for each field, from the C compiler."""
     import shutil
     import subprocess
     gcc = shutil.which("gcc")
     if gcc is None:
         pytest.skip("no C compiler")
-    fields = [f for f, _ in _native.Params._fields_]
-    src = tmp_path / "layout.c"
+    src = tmp_path / f"{struct}.c"
     src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "lqmc_gpu.h"\nint main(void) {\n'
-                   '    printf("%zu\\n", sizeof(lqmc_params));\n'
-                   + "".join(f'    printf("%zu\\n", offsetof(lqmc_params, {f}));\n' for f in fields)
+                   f'    printf("%zu\\n", sizeof({struct}));\n'
+                   + "".join(f'    printf("%zu\\n", offsetof({struct}, {f}));\n' for f in fields)
                    + "    return 0;\n}\n")
-    exe = tmp_path / "layout"
+    exe = tmp_path / struct
     r = subprocess.run([gcc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o",
                         str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     out = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
                                           check=True).stdout.split()]
-    assert out[0] == ctypes.sizeof(_native.Params)
-    assert out[1:] == [getattr(_native.Params, f).offset for f in fields]
+    return out[0], out[1:]
+
+
+def test_ctypes_params_layout_matches_the_c_struct(tmp_path):
+    """Every field of the binding's lqmc_params (and of the guide's stub) sits at the C
+    compiler's offset, and the sizes agree."""
+    import ctypes
+    fields = [f for f, _ in _native.Params._fields_]
+    size, offsets = _c_layout(tmp_path, "lqmc_params", fields)
+    assert size == ctypes.sizeof(_native.Params)
+    assert offsets == [getattr(_native.Params, f).offset for f in fields]
     with open(os.path.join(ROOT, "INTEGRATION.md")) as fh:
         stub = re.findall(r"```python\n(.*?)```", fh.read(), re.S)
     names = re.findall(r'\("(\w+)", ctypes\.c_', "".join(b for b in stub if "class Params" in b))
     assert names == fields
+
+
+def test_static_chain_binding_layout_matches_the_c_struct(tmp_path):
+    """The ctypes mirror of lqmc_static_chain that the allocation-free entry point's test
+    passes through the C ABI has the C compiler's layout."""
+    import ctypes
+    from test_zz_no_alloc import StaticChain
+    fields = [f for f, _ in StaticChain._fields_]
+    size, offsets = _c_layout(tmp_path, "lqmc_static_chain", fields)
+    assert size == ctypes.sizeof(StaticChain)
+    assert offsets == [getattr(StaticChain, f).offset for f in fields]
