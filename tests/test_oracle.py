@@ -196,3 +196,30 @@ def test_green_tau_oracle_matches_reference_exact_chain():
     for sigma in (1, -1):
         g = dqmc.green_tau(expm(-beta / L * K), 0.0, field, sigma)
         assert np.abs(g - f["gtau"]).max() < 1e-12
+
+
+@pytest.mark.parametrize("L,stabs", [(23, (1, 5, 23)), (7, (1, 3, 4))])
+def test_dqmc_ragged_refresh_chunks_agree(L, stabs):
+    """A slice count the refresh interval does not divide (a shorter last chunk) gives the same
+    decisions and G as refreshing every slice, and as one chunk for the whole sweep."""
+    K = kinetic_from_golden(2)
+    dt, U = 0.05, 4.0
+    lamb = np.arccosh(np.exp(U * dt / 2))
+    rng = np.random.default_rng(L)
+    field = (2 * rng.integers(0, 2, (4, L)) - 1).astype(np.int8)
+    uni = rng.random(3 * 4 * L)
+    runs = []
+    for stab in stabs:
+        ch = dqmc.Chain(expm(-dt * K), expm(dt * K), lamb, field.copy(), stab_every=stab)
+        out = []
+        for sw in range(3):
+            rec = {}
+            g = ch.sweep(uni[sw * 4 * L:(sw + 1) * 4 * L], record=rec)
+            out.append((rec["accept"].copy(), np.array(g)))
+        runs.append((out, ch.field.copy()))
+    (ref, f_ref), others = runs[0], runs[1:]
+    for out, f in others:
+        np.testing.assert_array_equal(f, f_ref)
+        for (acc, g), (acc0, g0) in zip(out, ref):
+            np.testing.assert_array_equal(acc, acc0)
+            assert np.abs(g - g0).max() < 1e-11
