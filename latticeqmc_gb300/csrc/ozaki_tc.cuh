@@ -53,6 +53,14 @@ constexpr int kStepB = kSlices * kTileB;
 constexpr int kMaxK = 512;                    // exact FP32 diagonal sums up to this k
 constexpr int kTmemCols = kSlices * kBN;      // 512: the whole tensor memory of the SM
 constexpr int kNonFinite = 1 << 20;
+
+// The epilogue drops the 12 low bits of the combined diagonals (so that the sum fits int64).
+// 0: floor them (a one-signed error below 2^-49 of 2^(E_i + F_j)); 1: round them to nearest
+// (half that, no bias).  The default is the measured configuration.
+#ifndef LQMC_OZ_ROUND_EPILOGUE
+#define LQMC_OZ_ROUND_EPILOGUE 0
+#endif
+constexpr long long kLowRound = LQMC_OZ_ROUND_EPILOGUE ? (1ll << 11) : 0;
 constexpr long long kWaitCycles = 2000000000ll;   // ~1 s of SM clock before a wait gives up
 
 // shared-memory bytes of `stages` stage buffers (1 or 2)
@@ -566,7 +574,7 @@ __device__ __forceinline__ void oz_gemm_tc_impl(double* c, int ldc, const double
                             hi = hi * (1 << kBits) + q[d];
                             lo = lo * (1 << kBits) + q[kSlices / 2 + d];
                         }
-                        const long long t = hi * (1ll << (kBits * kSlices / 2 - 12)) + (lo >> 12);
+                        const long long t = hi * (1ll << (kBits * kSlices / 2 - 12)) + ((lo + kLowRound) >> 12);
                         // C = T 2^(E_i + F_j - 2W + 7 (S - 1) + 12)
                         double v = 0.0;
                         if (t != 0) v = scaled_double(t, ei + ej[x] - 2 * kWidth + kBits * (kSlices - 1) + 12);

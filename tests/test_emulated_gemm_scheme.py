@@ -54,8 +54,10 @@ def digits(n):
     return np.stack(out)
 
 
-def emulated_product(a, b):
-    """C = A B through the digit scheme: A (m x k) split by rows, B (k x n) by columns."""
+def emulated_product(a, b, round_low=False):
+    """C = A B through the digit scheme: A (m x k) split by rows, B (k x n) by columns.
+    round_low: round the 12 dropped low bits to nearest (LQMC_OZ_ROUND_EPILOGUE=1) instead
+    of flooring them."""
     ea, eb = row_exponents(a), row_exponents(b.T)
     qa, qb = digits(fixed55(a, ea)), digits(fixed55(b.T, eb))      # (8, m, k), (8, n, k)
     d = np.zeros((SLICES,) + (a.shape[0], b.shape[1]), dtype=np.int64)
@@ -67,7 +69,7 @@ def emulated_product(a, b):
     for k in range(SLICES // 2):
         hi = hi * (1 << BITS) + d[k]
         lo = lo * (1 << BITS) + d[SLICES // 2 + k]
-    t_int = hi * (1 << (BITS * SLICES // 2 - 12)) + (lo >> 12)
+    t_int = hi * (1 << (BITS * SLICES // 2 - 12)) + ((lo + (2048 if round_low else 0)) >> 12)
     scale = ea[:, None] + eb[None, :] - 2 * WIDTH + BITS * (SLICES - 1) + 12
     return np.ldexp(t_int.astype(np.float64), scale), ea, eb, d
 
@@ -141,17 +143,18 @@ def test_product_within_float64_error_bound(m, k, n, span):
     assert worst * k <= 2.0 ** -49 + k * 4 * 2.0 ** -56, (worst, worst_plain)
 
 
-def test_epilogue_floor_is_one_signed_and_independent_of_k():
+@pytest.mark.parametrize("round_low", [False, True])
+def test_epilogue_drop_of_low_bits(round_low):
     """The combine floors the 12 low bits of sum_d D_d 2^(7 (7 - d)) (lo >> 12): against the
     same diagonals combined exactly, every product moves down by less than 2^-49 2^(E_i + F_j)
     (plus the final float64 rounding), whatever k is.  At small k this term dominates the
-    error, and it is a bias rather than noise; rounding instead of flooring would halve it and
-    remove the bias."""
+    error, and it is a bias rather than noise.  Rounding instead (LQMC_OZ_ROUND_EPILOGUE=1)
+    bounds the move by 2^-50 of 2^(E_i + F_j) in either direction and removes the bias."""
     rng = np.random.default_rng(7)
     for k in (4, 64):
         a = graded(rng, (12, k), 0)
         b = graded(rng, (12, k), 0).T.copy()
-        c, ea, eb, d = emulated_product(a, b)
+        c, ea, eb, d = emulated_product(a, b, round_low)
         shifts = []
         for i in range(12):
             for j in range(12):
@@ -159,7 +162,11 @@ def test_epilogue_floor_is_one_signed_and_independent_of_k():
                 unit = Fraction(2) ** (int(ea[i]) + int(eb[j]))
                 combined = Fraction(x) * Fraction(2) ** (BITS * (SLICES - 1) - 2 * WIDTH) * unit
                 shift = (Fraction(float(c[i, j])) - combined) / unit
-                assert -Fraction(2) ** -49 - abs(combined / unit) * Fraction(2) ** -53 <= shift
-                assert shift <= abs(combined / unit) * Fraction(2) ** -53
+                fl = abs(combined / unit) * Fraction(2) ** -53     # the final float64 rounding
+                lo, hi = (-Fraction(2) ** -50, Fraction(2) ** -50) if round_low else (-Fraction(2) ** -49, 0)
+                assert lo - fl <= shift <= hi + fl
                 shifts.append(float(shift))
-        assert np.mean(shifts) < -2.0 ** -52      # one-signed on average: a bias of ~2^-50
+        if round_low:
+            assert abs(np.mean(shifts)) < 2.0 ** -53     # no bias
+        else:
+            assert np.mean(shifts) < -2.0 ** -52         # one-signed: a bias of ~2^-50
