@@ -22,6 +22,8 @@ The result of ParallelProcessManager is the sweep-weighted mean over chains; the
 reference's unweighted mean over processes (lqmc/multiprocessing.py:265-267) differs from it
 only when the sweeps do not split evenly.
 """
+import os
+
 import numpy as np
 
 
@@ -76,14 +78,13 @@ class ParallelProcessManager(_Manager):
 class SerialProcessManager(_Manager):
     """G of one model at every beta of a list, one chain per beta."""
 
-    TMP_FILE = "tmp_gf_series.npz"
-
     def __init__(self, model, time_steps, warmup=300, sweeps=2000, det_mode=False, procs=None,
                  caching=True, **engine_kw):
         super().__init__(procs, model=model, time_steps=time_steps, warmup=warmup,
                          sweeps=sweeps, det_mode=det_mode)
         self.caching = caching
         self.engine_kw = engine_kw
+        self._tmp_file = "tmp_gf_series.npz"     # the cache measure_betas keeps while running
 
     def set_jobs(self, betas):
         self.var_kwargs = {"beta": np.atleast_1d(np.asarray(betas, dtype=np.float64))}
@@ -97,6 +98,10 @@ class SerialProcessManager(_Manager):
                                      caching=self.caching, det_mode=k["det_mode"],
                                      **self.engine_kw)
         self.result = np.swapaxes(np.array([gf_up, gf_dn]), 0, 1)
+
+    def delete_cache(self):
+        if os.path.isfile(self._tmp_file):
+            os.remove(self._tmp_file)
 
     def get_result(self):
         return self.result
