@@ -1,7 +1,7 @@
 """Throughput benchmark of the DQMC sweep engine on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload square16_beta8 | batched_fp64]
+                    [--workload square16_beta8 | batched_fp64 | square32_beta6]
 
 A step is one sweep of every chain of the workload (one lqmc_sweep(1) call).  The metric
 is site-updates/s: sum over chains of N_c * L_c site-update attempts per sweep, divided by
@@ -12,14 +12,19 @@ Workload square16_beta8 (default; the configuration the metric "batched mixed vs
 FP64 at max|dG| <= 1e-6" is quoted on): 64 chains of 16x16 (N=256), U=4, beta=8, dtau=0.1
 (L=80), dqmc, stabilisation every 8 slices, on-device Philox uniforms.  `value` is the
 batched mixed-precision engine that meets the max|dG| <= 1e-6 bar: precision "fp64e", every
-dense product (wraps, B-chain, delayed rank-k updates, the blocked QR's and the LU's
-updates) a float64-accurate GEMM emulated on the tcgen05 BF16 tensor cores, the per-site
-updates and panel factorisations in float64.  `fp64` carries the plain float64 engine on
+dense product (wraps, B-chain, delayed rank-k updates, the blocked QR's updates) a
+float64-accurate GEMM emulated on the tcgen05 BF16 tensor cores, the per-site updates,
+panel factorisations and the LU in float64.  `fp64` carries the plain float64 engine on
 the same workload (throughput and the speed-up of `value` over it) and `fp32_mixed` the
-float32 engine; both carry max|dG| against float64 on identical fields and uniforms.
+float32 engine; `accuracy` compares fp64e with fp64 over several sweeps from identical
+fields and uniforms.  Time-bounded sub-records of the other workloads ride on the same line:
+`batched_fp64` (512 uneven chains against the same chains run one at a time) and
+`square32_beta6` (32x32 chains, fp64e).
 
 Workload batched_fp64: 512 chains, 128 each of 4x4, 6x6, 8x8, 10x10, U drawn per chain
 from {2, 4, 6}, beta=4, L=40, dqmc float64, stabilisation every 5 slices.
+Workload square32_beta6: 32x32 (N=1024), U=4, beta=6, L=60, dqmc fp64e, stabilisation every
+10 slices, one chain per pair of SMs (one wave); the chain count HBM would admit is reported.
 
 value      device throughput with all state resident in HBM.
 e2e        the same sweeps through the public C ABI in replay mode (the drop-in path of
@@ -34,13 +39,18 @@ roofline   algorithmic float64 flops per sweep and chain
            workload: F / time against that DGEMM rate.
 cpu_baseline  the reference's fast sweep restated in Python/numpy (oracle/compat.py, with
            the pure-Python rank-1 loop of lqmc.py:328-331) on a bounded sample of every
-           lattice size of the workload, one process per host core.
+           lattice size of the workload, one process per host core; `single_process`
+           gives the same on one core.
+
+With --gpus N > 1 and no launcher environment, bench.py starts N ranks itself through
+torch.distributed.run (127.0.0.1); under a launcher, WORLD_SIZE must equal N.
 """
 import argparse
 import json
 import math
 import multiprocessing as mp
 import os
+import socket
 import statistics
 import subprocess
 import sys
@@ -53,13 +63,14 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "site-updates/s (sweeps/s beside it), DQMC sweep of batched Markov chains"
+UNIT = "site-updates/s"
 # DRAM traffic of one fp64e sweep launch of the square16_beta8 workload (64 chains), from ncu
 FP64E_TRAFFIC = 4.106e11
-UNIT = "site-updates/s"
+STATUS_BITS = {"nonfinite": 1, "singular": 2, "drift": 4, "timeout": 8}
 
 
 # ----------------------------------------------------------------------------------------
-# workload
+# workloads
 # ----------------------------------------------------------------------------------------
 def workload_batched(rank=0, per_side=128):
     from latticeqmc_gb300 import ChainSpec, HubbardModel
@@ -86,21 +97,26 @@ def workload_batched(rank=0, per_side=128):
     return specs, cfg
 
 
-def workload_square16(rank=0, chains=64):
+def workload_square(rank=0, chains=64, side=16, beta=8.0, L=80, stab=8, name="square16_beta8",
+                    precision="fp64e (value); fp64 and fp32 mixed reported beside it"):
     from latticeqmc_gb300 import ChainSpec, HubbardModel
-    side, beta, L, u = 16, 8.0, 80, 4.0
+    u = 4.0
     m = HubbardModel(u=u, t=1, mu=0)
     m.build_square(side)
     kin = m.ham_kinetic()
-    rng = np.random.default_rng(2000 + rank)
+    rng = np.random.default_rng(2000 + rank + 7919 * side)
     n = side * side
     specs = [ChainSpec(kin, u, beta, L, (2 * rng.integers(0, 2, (n, L)) - 1).astype(np.int8))
              for _ in range(chains)]
-    cfg = {"workload": f"square16_beta8: {chains} chains of 16x16 periodic (N=256), U=4, mu=0, "
-                       "beta=8, dtau=0.1 (L=80), dqmc, stab every 8, philox",
-           "chains": chains, "sides": [side], "beta": beta, "L": L, "stab_every": 8,
-           "precision": "fp64e (value); fp64 and fp32 mixed reported beside it", "mode": "dqmc"}
+    cfg = {"workload": f"{name}: {chains} chains of {side}x{side} periodic (N={n}), U=4, mu=0, "
+                       f"beta={beta:g}, dtau={beta / L:g} (L={L}), dqmc, stab every {stab}, philox",
+           "chains": chains, "sides": [side], "beta": beta, "L": L, "stab_every": stab,
+           "precision": precision, "mode": "dqmc"}
     return specs, cfg
+
+
+def workload_square16(rank=0, chains=64):
+    return workload_square(rank, chains)
 
 
 def algorithmic_flops(specs, accepted, stab_every):
@@ -109,6 +125,13 @@ def algorithmic_flops(specs, accepted, stab_every):
         n, L = c.n, c.L
         tot += 8.0 * L * n ** 3 + 4.0 * L * n ** 3 + 2.0 * math.ceil(L / stab_every) * (4.0 / 3.0) * n ** 3
     return tot + sum(4.0 * a * c.n ** 2 for a, c in zip(accepted, specs))
+
+
+def config_extras(world):
+    """Keys both arms add to the workload's config."""
+    return {"parallelism": f"chains sharded over {world} GPU(s)",
+            "l2": "working set (per-chain G, GEMM temporaries and UDT stacks; 0.6-1.6 GB) "
+                  "exceeds the 129 MB L2; no flush"}
 
 
 # ----------------------------------------------------------------------------------------
@@ -232,6 +255,7 @@ def cpu_baseline(specs, cfg, seconds_per_size=2.5, cores=None):
                    f"{cores} processes, {wall:.1f}s wall; extrapolated to one sweep of all "
                    f"{len(specs)} chains"),
         "sweep_seconds": per_sweep,
+        "wall_seconds": wall,
     }
 
 
@@ -256,11 +280,26 @@ def fp64_peak_tflops(torch):
     return best
 
 
+def status_counts(status):
+    """Chains with each LQMC_STATUS_* bit set, and with any bit set."""
+    st = np.asarray(status)
+    out = {f"chains_{k}": int(np.count_nonzero(st & b)) for k, b in STATUS_BITS.items()}
+    out["chains_flagged"] = int(np.count_nonzero(st))
+    return out
+
+
+def max_over_ranks(value, world):
+    if world <= 1:
+        return float(value)
+    from latticeqmc_gb300.distributed import max_over_ranks as mor
+    return mor(value)
+
+
 def time_engine(torch, specs, precision, stab, steps, warmup, stream, seed, dev, world,
-                sample_clocks=False):
+                sample_clocks=False, **engine_kw):
     from latticeqmc_gb300 import Engine
     eng = Engine(specs, mode="dqmc", precision=precision, rng="philox", seed=seed,
-                 stab_every=stab, device=dev)
+                 stab_every=stab, device=dev, **engine_kw)
     for _ in range(warmup):
         eng.sweep(1, stream=stream.cuda_stream)
     torch.cuda.synchronize()
@@ -281,17 +320,15 @@ def time_engine(torch, specs, precision, stab, steps, warmup, stream, seed, dev,
     end.synchronize()
     torch.cuda.synchronize()
     clk = clocks.stop() if clocks else None
-    ms = start.elapsed_time(end) / steps
+    ms = max_over_ranks(start.elapsed_time(end) / steps, world)
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
         torch.distributed.barrier()
     diags = [eng.diagnostics(c) for c in range(len(specs))]
     accepted = [(dg["accepted"] - a) / steps for a, dg in zip(acc0, diags)]
+    resid = [dg["max_residual"] for dg in diags]
     out = dict(ms=ms, launches=launches, clocks=clk, accepted=accepted,
-               resid=max(dg["max_residual"] for dg in diags),
-               status_bad=int(np.count_nonzero(eng.status() & 11)),
+               resid=max(resid), resid_median=float(np.median(resid)),
+               status=status_counts(eng.status()),
                phases={k: float(np.mean([dg["phase_cycles"][k] for dg in diags]))
                        for k in diags[0]["phase_cycles"]},
                subs={k: float(np.mean([dg["sub_cycles"][k] for dg in diags]))
@@ -300,35 +337,50 @@ def time_engine(torch, specs, precision, stab, steps, warmup, stream, seed, dev,
     return out
 
 
-def green_difference(specs, stab, dev, precision, sweeps=1):
-    """max|G_precision - G_fp64| after `sweeps` sweeps from identical fields and uniforms."""
+def green_difference(specs, stab, dev, precision, sweeps=1, seed=77):
+    """`precision` against fp64 over `sweeps` sweeps from identical fields and uniforms:
+    per sweep max|G_precision - G_fp64| over all chains and over the chains whose decisions
+    have all agreed so far (the pure precision effect), the number of such chains, and the
+    status bits and stabilisation residuals of both engines at the end."""
     from latticeqmc_gb300 import Engine
-    rng = np.random.default_rng(77)
+    rng = np.random.default_rng(seed)
     a = Engine(specs, mode="dqmc", precision="fp64", rng="replay", stab_every=stab, device=dev,
                record=True)
     b = Engine(specs, mode="dqmc", precision=precision, rng="replay", stab_every=stab, device=dev,
                record=True)
     total = sum(c.n * c.L for c in specs)
+    same = np.ones(len(specs), bool)
+    per_sweep, per_sweep_same = [], []
     for _ in range(sweeps):
         u = rng.random(total)
         a.set_uniforms_all(u)
         b.set_uniforms_all(u)
         a.sweep(1)
         b.sweep(1)
-    ga, gb = a.green_all(), b.green_all()
-    same = [bool(np.array_equal(a.decisions(c), b.decisions(c))) for c in range(len(specs))]
-    dg = float(np.abs(ga - gb).max())
-    # chains whose decisions all agreed: the pure precision effect
-    off, dg_same = 0, 0.0
-    for c, sp in enumerate(specs):
-        k = 2 * sp.n * sp.n
-        if same[c]:
-            dg_same = max(dg_same, float(np.abs(ga[off:off + k] - gb[off:off + k]).max()))
-        off += k
+        ga, gb = a.green_all(), b.green_all()
+        for c in range(len(specs)):
+            same[c] &= bool(np.array_equal(a.decisions(c), b.decisions(c)))
+        off, dg_same = 0, 0.0
+        for c, sp in enumerate(specs):
+            k = 2 * sp.n * sp.n
+            if same[c]:
+                dg_same = max(dg_same, float(np.abs(ga[off:off + k] - gb[off:off + k]).max()))
+            off += k
+        per_sweep.append(float(np.abs(ga - gb).max()))
+        per_sweep_same.append(dg_same if same.any() else None)
+    ra = [a.diagnostics(c)["max_residual"] for c in range(len(specs))]
+    rb = [b.diagnostics(c)["max_residual"] for c in range(len(specs))]
+    out = dict(max_dG=max(per_sweep),
+               max_dG_identical_decisions=(max(x for x in per_sweep_same if x is not None)
+                                           if same.any() else None),
+               max_dG_per_sweep=per_sweep, sweeps_compared=sweeps,
+               chains_with_identical_decisions=int(same.sum()), chains=len(specs),
+               status_fp64=status_counts(a.status()), status=status_counts(b.status()),
+               residual_fp64={"max": max(ra), "median": float(np.median(ra))},
+               residual={"max": max(rb), "median": float(np.median(rb))})
     a.close()
     b.close()
-    return dict(max_dG=dg, max_dG_identical_decisions=dg_same if any(same) else None,
-                chains_with_identical_decisions=int(sum(same)), chains=len(specs))
+    return out
 
 
 def time_e2e(torch, specs, stab, steps, warmup, stream, dev, world, rank, precision):
@@ -354,13 +406,74 @@ def time_e2e(torch, specs, stab, steps, warmup, stream, dev, world, rank, precis
         eng.sweep(1, stream=stream.cuda_stream)
         eng.green_all(g_np)
     torch.cuda.synchronize()
-    e2e_ms = (time.perf_counter() - t0) * 1e3 / steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks((time.perf_counter() - t0) * 1e3 / steps, world)
     eng.close()
     return e2e_ms, total_uni * 8, total_g * 8
+
+
+def batched_vs_sequential(torch, stream, dev, world, rank, steps=2, warmup=1, per_size_seq=4):
+    """The 512-chain uneven batch in its launches, against the same chains run one at a
+    time (one chain per launch), the latter timed on `per_size_seq` chains of each lattice
+    size and scaled to all 512 (the one-chain launch time does not depend on which chain of a
+    size it is)."""
+    from latticeqmc_gb300 import Engine
+    specs, cfg = workload_batched(rank, 128)
+    b = time_engine(torch, specs, "fp64", 5, steps, warmup, stream, 4242, dev, world)
+    sides = cfg["sides"]
+    seq_ms = 0.0
+    per_size = {}
+    for si, side in enumerate(sides):
+        mine = specs[si * 128: si * 128 + per_size_seq]
+        t = []
+        for sp in mine:
+            e = Engine([sp], mode="dqmc", precision="fp64", rng="philox", seed=5, stab_every=5,
+                       device=dev)
+            e.sweep(1, stream=stream.cuda_stream)
+            torch.cuda.synchronize()
+            s, en = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            e.sweep(1, stream=stream.cuda_stream)
+            en.record(stream)
+            en.synchronize()
+            t.append(s.elapsed_time(en))
+            e.close()
+        per_size[f"{side}x{side}"] = statistics.mean(t)
+        seq_ms += statistics.mean(t) * 128
+    sites = sum(c.n * c.L for c in specs)
+    return {"workload": cfg["workload"], "ms_per_step": b["ms"],
+            "value": sites * world / (b["ms"] * 1e-3), "unit": UNIT,
+            "sequential_ms_per_sweep": seq_ms, "sequential_value": sites / (seq_ms * 1e-3),
+            "speedup_vs_sequential": seq_ms / b["ms"],
+            "sequential_ms_per_chain_launch": per_size,
+            "sequential_sample": f"{per_size_seq} chains per size, one sweep each after one warm-up, "
+                                 "scaled by 128 chains per size",
+            "status": b["status"], "steps": steps, "warmup": warmup,
+            "gpu_launches": b["launches"]}
+
+
+def square32(torch, stream, dev, world, rank, steps=1, warmup=1):
+    """32x32, beta=6, L=60, fp64e, one chain per SM pair (one wave of the GPU)."""
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    chains = sms // 2
+    specs, cfg = workload_square(rank, chains, 32, 6.0, 60, 10, "square32_beta6", "fp64e")
+    r = time_engine(torch, specs, "fp64e", 10, steps, warmup, stream, 3232, dev, world)
+    free, _ = torch.cuda.mem_get_info(dev)
+    from latticeqmc_gb300 import Engine
+    one = Engine(specs[:1], mode="dqmc", precision="fp64e", rng="philox", stab_every=10, device=dev)
+    free1, _ = torch.cuda.mem_get_info(dev)
+    one.close()
+    per_chain = max(free - free1, 1)
+    sites = sum(c.n * c.L for c in specs)
+    flops = algorithmic_flops(specs, r["accepted"], 10)
+    return {"workload": cfg["workload"], "chains": chains, "ms_per_step": r["ms"],
+            "value": sites * world / (r["ms"] * 1e-3), "unit": UNIT,
+            "sweeps_per_s": 1e3 / r["ms"], "fp64_equivalent_tflops": flops / (r["ms"] * 1e-3) / 1e12,
+            "device_bytes_per_chain": per_chain,
+            "hbm_admits_chains": int(free // per_chain),
+            "note": "timed on one wave (one chain per SM pair); HBM would hold hbm_admits_chains, "
+                    "which run in waves of this size at this per-wave time",
+            "max_stabilisation_residual": r["resid"], "status": r["status"],
+            "steps": steps, "warmup": warmup, "gpu_launches": r["launches"]}
 
 
 def run_ours(args, rank, world):
@@ -369,159 +482,227 @@ def run_ours(args, rank, world):
     torch.cuda.set_device(dev)
     if args.workload == "batched_fp64":
         specs, cfg = workload_batched(rank, args.per_size)
+    elif args.workload == "square32_beta6":
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        specs, cfg = workload_square(rank, args.chains or sms // 2, 32, 6.0, 60, 10,
+                                     "square32_beta6", "fp64e")
     else:
-        specs, cfg = workload_square16(rank, args.chains)
+        specs, cfg = workload_square(rank, args.chains or 64)
     stab = cfg["stab_every"]
     stream = torch.cuda.Stream()
     seed = 12345 + 1000003 * rank
-    headline = "fp64e" if args.workload == "square16_beta8" else "fp64"
+    headline = "fp64" if args.workload == "batched_fp64" else "fp64e"
     main = time_engine(torch, specs, headline, stab, args.steps, args.warmup, stream, seed, dev,
                        world, sample_clocks=True)
-    others = {}
+    others, subs = {}, {}
     if args.workload == "square16_beta8":
-        dg = green_difference(specs, stab, dev, "fp64e")
-        main.update(dg)
+        acc = green_difference(specs, stab, dev, "fp64e", sweeps=args.accuracy_sweeps)
+        main["accuracy"] = acc
         for prec, key in (("fp64", "fp64"), ("mixed", "fp32_mixed")):
             o = time_engine(torch, specs, prec, stab, args.steps, args.warmup, stream, seed, dev, world)
-            od = dict(ms_per_step=o["ms"], status_flagged_chains=o["status_bad"],
+            od = dict(ms_per_step=o["ms"], status=o["status"],
                       max_stabilisation_residual=o["resid"])
             if prec != "fp64":
-                od.update(green_difference(specs, stab, dev, prec))
+                od.update(green_difference(specs, stab, dev, prec, sweeps=1))
             others[key] = od
+        if not args.no_subrecords:
+            subs["batched_fp64"] = batched_vs_sequential(torch, stream, dev, world, rank)
+            subs["square32_beta6"] = square32(torch, stream, dev, world, rank)
     e2e_ms, h2d, d2h = time_e2e(torch, specs, stab, args.steps, args.warmup, stream, dev, world,
                                 rank, headline)
     peak = fp64_peak_tflops(torch) if rank == 0 else None
     return dict(ms=main["ms"], sites=sum(c.n * c.L for c in specs), chains=len(specs),
                 flops=algorithmic_flops(specs, main["accepted"], stab), launches=main["launches"],
                 clocks=main["clocks"], e2e_ms=e2e_ms, h2d=h2d, d2h=d2h, cfg=cfg,
-                resid=main["resid"], status_bad=main["status_bad"], peak=peak, specs=specs,
-                phases=main["phases"], subs=main["subs"], others=others, headline=headline,
-                dg=dict((k, main[k]) for k in ("max_dG", "max_dG_identical_decisions",
-                                               "chains_with_identical_decisions", "chains")
-                        if k in main))
+                resid=main["resid"], resid_median=main["resid_median"], status=main["status"],
+                peak=peak, specs=specs, phases=main["phases"], subs_cycles=main["subs"],
+                others=others, subrecords=subs, headline=headline,
+                accuracy=main.get("accuracy"))
 
 
-def main():
+def roofline(r, args):
+    fp64_eq = r["flops"] / (r["ms"] * 1e-3) / 1e12
+    if r["headline"] == "fp64e":
+        peaks = {}
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                peaks = json.load(f)
+        except (OSError, ValueError):
+            pass
+        tpeak = peaks.get("bf16_tflops_sustained")
+        tsrc = "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"
+        if tpeak is None:
+            tpeak, tsrc = 1700.0, "fallback sustained bf16 figure (of fallback)"
+        achieved = 36.0 * fp64_eq
+        full = args.workload == "square16_beta8" and (args.chains or 64) == 64
+        roof = {"bound": "tensor", "achieved": achieved, "peak": tpeak, "unit": "TFLOP/s",
+                "frac": achieved / tpeak, "peak_source": tsrc,
+                "traffic": FP64E_TRAFFIC if full else None,
+                "traffic_unit": "DRAM bytes per launch (one sweep of all chains)",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
+                                  "fp64e sweep kernel on this workload (mean of 2 launches)",
+                "kernel": "sweep kernel of the fp64e engine (BF16 slice products: 36 per "
+                          "algorithmic float64 flop)",
+                "fp64_equivalent": {"achieved": fp64_eq, "peak": r["peak"], "unit": "TFLOP/s",
+                                    "frac": fp64_eq / r["peak"] if r["peak"] else None,
+                                    "peak_source": "cuBLAS DGEMM 4096^3 measured in this run"}}
+        dtype = "f64 (GEMMs emulated: 8 BF16 slices, FP32 tensor-core accumulation)"
+    else:
+        roof = {"bound": "fp64", "achieved": fp64_eq, "peak": r["peak"], "unit": "TFLOP/s",
+                "frac": fp64_eq / r["peak"] if r["peak"] else None, "traffic": None,
+                "peak_source": "cuBLAS DGEMM 4096^3 measured in this run "
+                               "(MEASURED_PEAKS.json carries no float64 figure)",
+                "kernel": "sweep kernel of the float64 engine (all launch buckets of one sweep)"}
+        dtype = "f64"
+    return roof, dtype
+
+
+def make_line(args, r, world, cpu):
+    """The JSON line rank 0 prints from its (max-over-ranks) measurements."""
+    sites_all = r["sites"] * world
+    value = sites_all / (r["ms"] * 1e-3)
+    e2e = sites_all / (r["e2e_ms"] * 1e-3)
+    roof, dtype = roofline(r, args)
+    tot = max(sum(r["phases"].values()), 1.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"],
+        "sweeps_per_s": 1e3 / r["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+        "config": dict(r["cfg"], **config_extras(world)),
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
+                "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"]},
+        "gpu_launches": r["launches"],
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "clocks": r["clocks"],
+        "status": dict(r["status"], max_stabilisation_residual=r["resid"],
+                       median_stabilisation_residual=r["resid_median"]),
+        "phase_share": {k: v / tot for k, v in r["phases"].items()},
+        "sub_share": {k: v / tot for k, v in r["subs_cycles"].items()},
+    }
+    if r.get("accuracy"):
+        acc = dict(r["accuracy"])
+        acc["meets_max_dG_1e-6"] = bool(acc["max_dG"] <= 1e-6)
+        line["accuracy"] = acc
+    for key, od in r["others"].items():
+        entry = dict(od, value=sites_all / (od["ms_per_step"] * 1e-3), unit=UNIT)
+        if key == "fp64":
+            entry["speedup_of_value"] = od["ms_per_step"] / r["ms"]
+        else:
+            entry["speedup_vs_fp64"] = r["others"]["fp64"]["ms_per_step"] / od["ms_per_step"]
+            entry["meets_max_dG_1e-6"] = bool(od["max_dG"] <= 1e-6)
+        line[key] = entry
+    line.update(r["subrecords"])
+    return line
+
+
+def reference_arm(args):
+    """The reference's CPU path (the port) on the host cores: each step is one bounded
+    sample of every lattice size on every core; `value` is the per-site rate of the samples
+    applied to one sweep of the workload, `ms_per_step` the wall time of a step."""
+    if args.workload == "batched_fp64":
+        specs, cfg = workload_batched(0, args.per_size)
+    elif args.workload == "square32_beta6":
+        specs, cfg = workload_square(0, args.chains or 76, 32, 6.0, 60, 10, "square32_beta6", "fp64e")
+    else:
+        specs, cfg = workload_square(0, args.chains or 64)
+    vals, walls = [], []
+    last = None
+    for s in range(args.warmup + args.steps):
+        last = cpu_baseline(specs, cfg, seconds_per_size=min(args.cpu_seconds, 1.0))
+        if s >= args.warmup:
+            vals.append(last["value"])
+            walls.append(last["wall_seconds"])
+    v = statistics.mean(vals)
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": statistics.mean(walls) * 1e3,
+            "step": "one bounded sample of the reference's sweep on every host core (the rate "
+                    "is the slope between two sample lengths, applied to one sweep of all chains)",
+            "sweep_seconds_extrapolated": sum(c.n * c.L for c in specs) / v,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "config": dict(cfg, **config_extras(1)),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"],
+                             "kind": "port", "sample": last["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def launcher_command(argv, gpus, port=None):
+    """torch.distributed.run command that starts `gpus` ranks of this script on 127.0.0.1."""
+    if port is None:
+        with socket.socket() as s:
+            s.bind(("127.0.0.1", 0))
+            port = s.getsockname()[1]
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1",
+            f"--nproc-per-node={gpus}", "--master-addr", "127.0.0.1", f"--master-port={port}",
+            os.path.abspath(__file__), *argv]
+
+
+def check_world(gpus, env):
+    """World size of this process: `gpus` must match the launcher's WORLD_SIZE if one is
+    set.  Returns None when bench.py has to start the ranks itself."""
+    if "WORLD_SIZE" not in env:
+        return None if gpus > 1 else 1
+    world = int(env["WORLD_SIZE"])
+    if world != gpus:
+        raise SystemExit(f"bench.py: --gpus {gpus} but the launcher started {world} ranks")
+    return world
+
+
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="square16_beta8", choices=["square16_beta8", "batched_fp64"])
-    ap.add_argument("--chains", type=int, default=64, help="chains of the square16_beta8 workload")
+    ap.add_argument("--workload", default="square16_beta8",
+                    choices=["square16_beta8", "batched_fp64", "square32_beta6"])
+    ap.add_argument("--chains", type=int, default=0,
+                    help="chains of the square workloads (0: 64 at 16x16, one wave at 32x32)")
+    ap.add_argument("--accuracy-sweeps", type=int, default=10,
+                    help="sweeps of the fp64e-vs-fp64 comparison from identical inputs")
     ap.add_argument("--cpu-seconds", type=float, default=2.5,
                     help="seconds of CPU sampling per lattice size and process")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-subrecords", action="store_true",
+                    help="leave out the batched_fp64 and square32_beta6 sub-records")
     ap.add_argument("--per-size", type=int, default=128,
                     help="chains per lattice size (128 is the workload; smaller for profiling)")
-    args = ap.parse_args()
-    world = int(os.environ.get("WORLD_SIZE", "1"))
+    return ap.parse_args(argv)
+
+
+def main(argv=None):
+    argv = sys.argv[1:] if argv is None else argv
+    args = parse(argv)
+    world = check_world(args.gpus, os.environ)
+    if world is None:
+        return subprocess.call(launcher_command(argv, args.gpus))
     rank = int(os.environ.get("RANK", "0"))
-
     if args.impl == "reference":
-        if rank != 0:
-            return
-        if args.workload == "batched_fp64":
-            specs, cfg = workload_batched(0, args.per_size)
-        else:
-            specs, cfg = workload_square16(0, args.chains)
-        vals = []
-        last = None
-        for s in range(args.warmup + args.steps):
-            last = cpu_baseline(specs, cfg, seconds_per_size=min(args.cpu_seconds, 1.0))
-            if s >= args.warmup:
-                vals.append(last["value"])
-        v = statistics.mean(vals)
-        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
-                "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": sum(c.n * c.L for c in specs) / v * 1e3,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64", "data": "synthetic", "config": cfg,
-                "cpu_baseline": {"value": v, "unit": UNIT, "cores": last["cores"],
-                                 "kind": "port", "sample": last["sample"]},
-                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
-        return
-
+        if rank == 0:
+            print(json.dumps(reference_arm(args)))
+        return 0
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl")
     r = run_ours(args, rank, world)
-    sites_all = r["sites"] * world
-    value = sites_all / (r["ms"] * 1e-3)
-    e2e = sites_all / (r["e2e_ms"] * 1e-3)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(r["specs"], r["cfg"], seconds_per_size=args.cpu_seconds)
-        cpu.pop("sweep_seconds", None)
+        one = cpu_baseline(r["specs"], r["cfg"], seconds_per_size=args.cpu_seconds, cores=1)
+        for d in (cpu, one):
+            d.pop("sweep_seconds", None)
+            d.pop("wall_seconds", None)
+        cpu["single_process"] = {k: one[k] for k in ("value", "unit", "cores", "sample")}
     if rank == 0:
-        fp64_eq = r["flops"] / (r["ms"] * 1e-3) / 1e12
-        if r["headline"] == "fp64e":
-            peaks = {}
-            try:
-                with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-                    peaks = json.load(f)
-            except (OSError, ValueError):
-                pass
-            tpeak = peaks.get("bf16_tflops_sustained")
-            tsrc = "MEASURED_PEAKS.json bf16_tflops_sustained (of measured)"
-            if tpeak is None:
-                tpeak, tsrc = 1700.0, "fallback sustained bf16 figure (of fallback)"
-            achieved = 36.0 * fp64_eq
-            roof = {"bound": "tensor", "achieved": achieved, "peak": tpeak, "unit": "TFLOP/s",
-                    "frac": achieved / tpeak, "peak_source": tsrc,
-                    "traffic": FP64E_TRAFFIC if args.chains == 64 else None,
-                    "traffic_unit": "DRAM bytes per launch (one sweep of all chains)",
-                    "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the "
-                                      "fp64e sweep kernel on this workload (mean of 2 launches)",
-                    "kernel": "sweep kernel of the fp64e engine (BF16 slice products: 36 per "
-                              "algorithmic float64 flop)",
-                    "fp64_equivalent": {"achieved": fp64_eq, "peak": r["peak"], "unit": "TFLOP/s",
-                                        "frac": fp64_eq / r["peak"] if r["peak"] else None,
-                                        "peak_source": "cuBLAS DGEMM 4096^3 measured in this run"}}
-            dtype = "f64 (GEMMs emulated: 8 BF16 slices, FP32 tensor-core accumulation)"
-        else:
-            roof = {"bound": "fp64", "achieved": fp64_eq, "peak": r["peak"], "unit": "TFLOP/s",
-                    "frac": fp64_eq / r["peak"] if r["peak"] else None, "traffic": None,
-                    "peak_source": "cuBLAS DGEMM 4096^3 measured in this run "
-                                   "(MEASURED_PEAKS.json carries no float64 figure)",
-                    "kernel": "sweep kernel of the float64 engine (all launch buckets of one sweep)"}
-            dtype = "f64"
-        line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"],
-            "sweeps_per_s": 1e3 / r["ms"], "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": dtype, "data": "synthetic",
-            "config": dict(r["cfg"], parallelism=f"chains sharded over {world} GPU(s)",
-                           l2="working set (per-chain G, GEMM temporaries and UDT stacks; "
-                              "0.6-1.6 GB) exceeds the 129 MB L2; no flush"),
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
-                    "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"]},
-            "gpu_launches": r["launches"],
-            "roofline": roof,
-            "cpu_baseline": cpu,
-            "clocks": r["clocks"],
-            "accuracy": dict({"max_stabilisation_residual": r["resid"],
-                              "chains_with_status_flags": r["status_bad"]}, **r["dg"]),
-            "phase_share": {k: v / max(sum(r["phases"].values()), 1.0) for k, v in r["phases"].items()},
-            "sub_share": {k: v / max(sum(r["phases"].values()), 1.0) for k, v in r["subs"].items()},
-        }
-        if "max_dG" in r["dg"]:
-            line["accuracy"]["meets_max_dG_1e-6"] = bool(r["dg"]["max_dG"] <= 1e-6)
-        for key, od in r["others"].items():
-            entry = dict(od, value=sites_all / (od["ms_per_step"] * 1e-3), unit=UNIT)
-            if key == "fp64":
-                entry["speedup_of_value"] = od["ms_per_step"] / r["ms"]
-            else:
-                entry["speedup_vs_fp64"] = r["others"]["fp64"]["ms_per_step"] / od["ms_per_step"]
-                entry["meets_max_dG_1e-6"] = bool(od["max_dG"] <= 1e-6)
-            line[key] = entry
-        print(json.dumps(line))
+        print(json.dumps(make_line(args, r, world, cpu)))
     if world > 1:
         import torch
         torch.distributed.destroy_process_group()
+    return 0
 
 
 if __name__ == "__main__":
-    main()
+    sys.exit(main())

@@ -70,7 +70,20 @@ def _run_batch(specs, warmup, per_chain_sweeps, mode, rng, seed, engine_kw):
             raise ValueError("batched runs draw their uniforms on the device (rng='philox')")
         eng.sweep(warmup, measure=False)
         eng.reset_measurements()
-        eng.sweep(int(np.max(per_chain_sweeps)), measure=True)
+        # every chain is measured for exactly its share: all chains sweep together, and a
+        # chain whose share is used up keeps the sums it had then (the extra sweeps of
+        # the longer shares still advance it, unmeasured in effect)
+        per = np.asarray(per_chain_sweeps, dtype=np.int64)
+        done, kept = 0, {}
+        for share in np.unique(per):
+            if share > done:
+                eng.sweep(int(share - done), measure=True)
+                done = int(share)
+            for c in np.nonzero(per == share)[0]:
+                if share < per.max():
+                    kept[int(c)] = (eng.green_sum(int(c))[0], eng.observables_raw(int(c)))
+        for c, (gsum, obs) in kept.items():
+            eng.set_measurement_sums(c, gsum, obs)
         results = []
         for c in range(len(specs)):
             gsum, cnt = eng.green_sum(c)

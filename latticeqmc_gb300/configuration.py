@@ -46,15 +46,6 @@ class Configuration:
     def __getitem__(self, item):
         return self.config[item]
 
-    def string_header(self, delim=" "):
-        return r"i\l  " + delim.join([f"{i:^3}" for i in range(self.time_steps)])
-
-    def string_bulk(self, delim=" "):
-        rows = []
-        for site in range(self.n_sites):
-            row = delim.join([f"{x:^3}" for x in self.config[site, :]])
-            rows.append(f"{site:<3} [{row}]")
-        return "\n".join(rows)
-
-    def __str__(self):
-        return self.string_header() + "\n" + self.string_bulk()
+    def __repr__(self):
+        return (f"Configuration(n_sites={self.n_sites}, time_steps={self.time_steps}, "
+                f"mean={float(np.mean(self.config)):+.3f})")

@@ -74,6 +74,12 @@ def run_local_chains(specs, warmup, sweeps, rank, world, seed=0, **engine_kw):
     Returns (mean G, mean observables vector, total measurements) over every chain of every
     rank.  All ranks must pass the same `specs` list."""
     from .engine import Engine
+    # every rank checks the same condition on the same `specs` before any collective, so
+    # too few chains raise the same error everywhere instead of leaving ranks waiting in
+    # the final all_reduce
+    if len(specs) < world:
+        raise ValueError(f"{len(specs)} chains cannot be shared by {world} ranks: every rank "
+                         "needs at least one chain")
     mine = [specs[i] for i in shard_chains(len(specs), rank, world)]
     eng = Engine(mine, rng="philox", seed=rank_seed(seed, rank), **engine_kw)
     try:

@@ -222,6 +222,13 @@ class Engine:
             "szsz": o[h + 2 * n + n * n:h + 2 * n + 2 * n * n].reshape(n, n) / cnt,
         }
 
+    def set_measurement_sums(self, chain, green_sum, obs):
+        """Overwrite a chain's sum of G (2, N, N) and its observable sums (the count in
+        obs[0] included), e.g. to drop measurements taken after its share of sweeps."""
+        g = as_f64(green_sum)
+        o = as_f64(obs)
+        self._h.call("lqmc_set_chain_state", int(chain), None, ptr(g), ptr(o))
+
     def reset_measurements(self):
         self._h.call("lqmc_reset_measurements")
 

@@ -48,42 +48,63 @@ def local_gf(gf):
 
 
 def matsubara_frequencies(points, beta):
-    n_points = np.asanyarray(points).astype(dtype=int, casting="safe")
-    return 1j * np.pi / beta * (2 * n_points + 1)
+    """Fermionic Matsubara frequencies i w_n = i pi (2 n + 1) / beta for integer points n
+    (lqmc/tools.py:125-142; non-integer points raise TypeError)."""
+    n = np.asanyarray(points).astype(dtype=int, casting="safe")
+    return (2 * n + 1) * (1j * np.pi / beta)
+
+
+def _softplus(z):
+    """log(1 + e^z), elementwise, real or complex, without overflow: the branch on Re z
+    keeps the exponential's argument non-positive."""
+    z = np.asanyarray(z)
+    pos = z.real > 0
+    zz = np.where(pos, -z, z)
+    return np.where(pos, z, 0) + np.log1p(np.exp(zz))
 
 
 def fermi_fct(eps, beta):
-    """1 / (exp(beta eps) + 1) (lqmc/tools.py:145-162)."""
-    return 0.5 * (1. + np.tanh(-0.5 * beta * eps))
+    """Fermi function 1 / (e^{beta eps} + 1) (lqmc/tools.py:145-162), evaluated as
+    exp(-softplus(beta eps)) so that neither sign of beta eps overflows; same type as eps."""
+    val = np.exp(-_softplus(beta * np.asanyarray(eps)))
+    return val if np.ndim(val) else val[()]
 
 
 def decompose(a):
+    """Eigen-decomposition of the Hermitian matrix a = rv diag(xi) rv_inv
+    (lqmc/tools.py:168-170).  rv is unitary, so rv_inv is its conjugate transpose."""
     xi, rv = np.linalg.eigh(a)
-    return rv, xi, np.linalg.inv(rv)
+    return rv, xi, np.conj(np.swapaxes(rv, -1, -2))
 
 
 def reconstruct(rv, xi, rv_inv, diag=False):
+    """rv diag(xi) rv_inv for every leading index of xi (..., N), or only its diagonal
+    (lqmc/tools.py:173-177)."""
     if diag:
-        return ((np.transpose(rv_inv) * rv) @ xi[..., np.newaxis])[..., 0]
-    return (rv * xi[..., np.newaxis, :]) @ rv_inv
+        return np.einsum("ik,...k,ki->...i", rv, xi, rv_inv)
+    return np.einsum("ik,...k,kj->...ij", rv, xi, rv_inv)
 
 
 def pole_gf_tau(tau, poles, weights, beta):
-    """Imaginary-time G of a sum of poles (lqmc/tools.py:182-190)."""
+    """G(tau) = -sum_p w_p e^{-tau p} / (1 + e^{-beta p}) of a sum of poles, 0 <= tau <= beta
+    (lqmc/tools.py:182-190).  Each term is exp(-tau p - softplus(-beta p)), finite for
+    either sign of Re p.  tau's shape comes first, then poles' leading axes; the last pole
+    axis is summed."""
     assert np.all((tau >= 0.) & (tau <= beta))
     poles, weights = np.atleast_1d(*np.broadcast_arrays(poles, weights))
     tau = np.asanyarray(tau)
-    tau = tau.reshape(tau.shape + (1,) * poles.ndim)
-    exponent = np.where(poles.real >= 0, -tau, beta - tau) * poles
-    single_pole_tau = np.exp(exponent) * fermi_fct(-np.sign(poles.real) * poles, beta)
-    return -np.sum(weights * single_pole_tau, axis=-1)
+    t = tau.reshape(tau.shape + (1,) * poles.ndim)
+    terms = np.exp(-t * poles - _softplus(-beta * poles))
+    return -np.sum(weights * terms, axis=-1)
 
 
 def compute_pole_gf_tau(ham, beta):
-    """Non-interacting G(tau) of the one-body Hamiltonian ``ham`` (lqmc/tools.py:193-200)."""
-    rv, xi, rv_inv = decompose(ham)
+    """Non-interacting imaginary-time G(tau) of the one-body Hamiltonian ``ham`` on 2049
+    points of [0, beta] (lqmc/tools.py:193-200): G(tau) = -V diag(e^{-tau e} / (1 +
+    e^{-beta e})) V^T from ham = V diag(e) V^T.  Returns (tau, G) with G of shape
+    (N, N, 2049)."""
+    energies, vecs = np.linalg.eigh(ham)
     tau = np.linspace(0, beta, num=2049)
-    diag_gf_tau = pole_gf_tau(tau, xi[..., np.newaxis], weights=1, beta=beta)
-    gf_tau = reconstruct(rv, diag_gf_tau, rv_inv)
-    gf_tau = np.moveaxis(gf_tau, 0, -1)
-    return tau, gf_tau
+    occ = pole_gf_tau(tau, energies[:, None], weights=1, beta=beta)      # (2049, N)
+    g = np.einsum("ik,tk,jk->ijt", vecs, occ, np.conj(vecs))
+    return tau, g

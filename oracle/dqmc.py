@@ -66,13 +66,21 @@ def householder_qr(z):
     return q, np.triu(z), (-1.0) ** nrefl
 
 
-def udt_step(z_times_u, d, t):
+def lapack_qr(z):
+    """The same Householder QR through LAPACK (numpy.linalg.qr: dgeqrf/dorgqr, whose
+    reflectors follow the same beta = -sign(alpha) ||x|| convention), for large matrices
+    where the Python loop of householder_qr is slow.  Returns (q, r, det_q_sign)."""
+    q, r = np.linalg.qr(z)
+    return q, r, float(np.linalg.slogdet(q)[0])
+
+
+def udt_step(z_times_u, d, t, qr=householder_qr):
     """Absorb a left factor: given Z = C U (U of the old decomposition), return the UDT of
     C U diag(d) T with pre-pivoting by column norms of Z diag(d)."""
     zd = z_times_u * d[None, :]
     norms = np.sqrt(np.sum(zd * zd, axis=0))
     order = np.argsort(-norms, kind="stable")
-    q, r, sq = householder_qr(zd[:, order])
+    q, r, sq = qr(zd[:, order])
     dn = np.diag(r).copy()
     tn = (r / dn[:, None]) @ t[order, :]
     return q, dn, tn, sq
@@ -105,7 +113,8 @@ def identity_udt(n):
 class Chain:
     """One Markov chain of the textbook DQMC (both spins)."""
 
-    def __init__(self, exp_k, exp_k_inv, lamb, field, stab_every, kinetic=None, u=0.0):
+    def __init__(self, exp_k, exp_k_inv, lamb, field, stab_every, kinetic=None, u=0.0,
+                 delay=0, qr="householder"):
         self.exp_k = np.asarray(exp_k, dtype=np.float64)
         self.exp_k_inv = np.asarray(exp_k_inv, dtype=np.float64)
         self.lamb = float(lamb)
@@ -118,6 +127,13 @@ class Chain:
         self.max_resid = 0.0
         self.logdet = np.zeros(2)
         self.sign = np.ones(2)
+        # delay > 0: the accepted flips of a slice are applied as delayed rank-k updates
+        # (G_eff = G - X Y^T, flushed every `delay` flips and at the end of each slice),
+        # the same algebra as the rank-1 update in another order of operations; qr =
+        # "lapack" factors the UDT steps through LAPACK.  Both only make large lattices
+        # fast enough to check; the defaults are the pinned restatement.
+        self.delay = int(delay)
+        self.qr = lapack_qr if qr == "lapack" else householder_qr
 
     def b_left(self, l, sigma, z):
         """B_l z = exp_v(l) exp_k z."""
@@ -135,7 +151,7 @@ class Chain:
             z = u
             for l in range(lo, hi):
                 z = self.b_left(l, sigma, z)
-            u, d, t, sq = udt_step(z, d, t)
+            u, d, t, sq = udt_step(z, d, t, self.qr)
             s = sq
             stack.append((u, d, t, s))
         return stack
@@ -145,7 +161,7 @@ class Chain:
         z = u
         for l in reversed(range(lo, hi)):
             z = self.bt_left(l, sigma, z)
-        u, d, t, sq = udt_step(z, d, t)
+        u, d, t, sq = udt_step(z, d, t, self.qr)
         return (u, d, t, sq)
 
     def wrap(self, l, g, sigma):
@@ -171,6 +187,11 @@ class Chain:
             lo, hi = ch[c]
             for l in reversed(range(lo, hi)):
                 step = L - 1 - l
+                if self.delay > 0:
+                    pos = self._update_slice_delayed(g, l, step, uniforms, pos, acc_rec, rat_rec)
+                    if l > 0:
+                        g = [self.wrap(l, g[0], +1), self.wrap(l, g[1], -1)]
+                    continue
                 for i in range(n):
                     s_il = self.field[i, l]
                     dl_up = np.exp(2.0 * self.lamb * s_il) - 1.0
@@ -205,6 +226,49 @@ class Chain:
             record["accept"] = acc_rec
             record["ratio"] = rat_rec
         return self.green
+
+
+def _slice_delayed(self, g, l, step, uniforms, pos, acc_rec, rat_rec):
+    """Site updates of slice l with delayed rank-k updates: x = G_eff[:, i],
+    y = (Delta/R)(e_i - G_eff[i, :]) with G_eff = G - X Y^T; G -= X Y^T every `delay`
+    accepted flips and at the end of the slice.  Same ratio, acceptance and uniform per
+    site as the rank-1 loop of ``sweep``."""
+    n, k = self.n, self.delay
+    xs = [np.zeros((n, k)), np.zeros((n, k))]
+    ys = [np.zeros((n, k)), np.zeros((n, k))]
+    m = 0
+    for i in range(n):
+        s_il = self.field[i, l]
+        dls = (np.exp(2.0 * self.lamb * s_il) - 1.0, np.exp(-2.0 * self.lamb * s_il) - 1.0)
+        gii = [g[s][i, i] - xs[s][i, :m] @ ys[s][i, :m] for s in range(2)]
+        rs = [1.0 + dls[s] * (1.0 - gii[s]) for s in range(2)]
+        ratio = rs[0] * rs[1]
+        acc = uniforms[pos] <= ratio
+        pos += 1
+        acc_rec[step, i] = acc
+        rat_rec[step, i] = ratio
+        if not acc:
+            continue
+        for s in range(2):
+            x = g[s][:, i] - xs[s][:, :m] @ ys[s][i, :m]
+            row = g[s][i, :] - xs[s][i, :m] @ ys[s][:, :m].T
+            y = -row
+            y[i] += 1.0
+            xs[s][:, m] = x
+            ys[s][:, m] = y * (dls[s] / rs[s])
+        self.field[i, l] = -s_il
+        m += 1
+        if m == k:
+            for s in range(2):
+                g[s] = g[s] - xs[s] @ ys[s].T
+            m = 0
+    if m:
+        for s in range(2):
+            g[s] = g[s] - xs[s][:, :m] @ ys[s][:, :m].T
+    return pos
+
+
+Chain._update_slice_delayed = _slice_delayed
 
 
 def green_tau(exp_k, lamb, field, sigma):

@@ -1,8 +1,8 @@
 """Time the reference's own fast sweep (lqmc/lqmc.py:301-347) against the CPU port that the
 bench reports as its baseline (oracle/compat.py), on one core with one BLAS thread.
 
-Test infrastructure, not product: it imports the reference from LQMC_REFERENCE (default
-/root/reference), so it runs only where the reference is present.
+Test infrastructure, not product: it imports the reference from the directory named by the
+LQMC_REFERENCE environment variable (required), so it runs only where the reference is present.
 
 Workload: periodic 16x16 square lattice, t = 1, U = 4, mu = 0, dtau = 0.1. The reference's
 lattice builder cannot close a 16x16 periodic lattice (lqmc/lattice.py:1030-1031), so a
@@ -23,7 +23,9 @@ import types
 
 import numpy as np
 
-REF = os.environ.get("LQMC_REFERENCE", "/root/reference")
+REF = os.environ.get("LQMC_REFERENCE")
+if not REF:
+    raise SystemExit("set LQMC_REFERENCE to the directory that holds the reference's lqmc package")
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 

@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this folder by running the reference lqmc package.
 
 The reference (KieDani/LatticeQMC, package ``lqmc``) is pure Python.  It is read from
-``LQMC_REFERENCE`` (default ``/root/reference``) and imported with stub modules for
+the directory named by the ``LQMC_REFERENCE`` environment variable (required) and imported with stub modules for
 matplotlib, which it imports at module top only for plotting
 (``lqmc/lattice.py:11-13``, ``lqmc/configuration.py:9``).
 
@@ -36,7 +36,9 @@ import numpy as np
 from scipy.linalg import expm
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("LQMC_REFERENCE", "/root/reference")
+REF = os.environ.get("LQMC_REFERENCE")
+if not REF:
+    raise SystemExit("set LQMC_REFERENCE to the directory that holds the reference's lqmc package")
 
 
 def _install_matplotlib_stub():

@@ -78,3 +78,32 @@ def test_two_gloo_ranks_merge_to_the_single_process_answer(tmp_path):
         np.testing.assert_allclose(f["omean"], np.arange(4.0) * cnt.sum() / cnt.sum())
         assert int(f["total"]) == cnt.sum()
         assert float(f["tmax"]) == 11.0
+
+
+def _worker_too_few(rank, world, port, out_dir):
+    import torch.distributed as dist
+    from latticeqmc_gb300.distributed import run_local_chains
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        raised = ""
+        try:
+            # one chain for two ranks: every rank must refuse before building an engine or
+            # entering a collective
+            run_local_chains([object()], warmup=1, sweeps=1, rank=rank, world=world)
+        except ValueError as e:
+            raised = str(e)
+        dist.barrier()
+        np.savez(os.path.join(out_dir, f"few{rank}.npz"), raised=raised)
+    finally:
+        dist.destroy_process_group()
+
+
+def test_fewer_chains_than_ranks_raises_on_every_rank(tmp_path):
+    import torch.multiprocessing as tmp
+    world = 2
+    tmp.spawn(_worker_too_few, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True)
+    for r in range(world):
+        msg = str(np.load(tmp_path / f"few{r}.npz")["raised"])
+        assert "cannot be shared by 2 ranks" in msg

@@ -111,8 +111,9 @@ def test_mixed_precision_2x2_observables_match_exact_diagonalisation():
 
 @pytest.mark.parametrize("side,beta,L,stab", [(4, 4.0, 40, 5), (8, 4.0, 80, 10), (12, 4.0, 40, 5)])
 def test_fp64e_matches_oracle(side, beta, L, stab):
-    """Every dense product on the BF16 tensor cores with 48-bit sliced operands: decisions
-    as the float64 oracle, G within the wrap-amplified truncation error (1e-8)."""
+    """Every dense product on the BF16 tensor cores, operands carried as 55-bit fixed-point
+    integers in eight BF16 digits: decisions as the float64 oracle, G within the
+    wrap-amplified rounding error (1e-8)."""
     K, field, rng = _setup(side, beta, L, 500 + side)
     N = side * side
     spec = ChainSpec(K, 4.0, beta, L, field)

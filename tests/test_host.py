@@ -70,7 +70,7 @@ def test_configuration_draws_like_reference():
     c.update(1, 2)
     assert c[1, 2] == -ref[1, 2]
     assert c.copy() == c
-    assert "i\\l" in str(c)
+    assert "n_sites=5" in repr(c)
 
 
 def test_engine_constants_match_reference_forms():
