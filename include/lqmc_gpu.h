@@ -61,6 +61,14 @@ extern "C" {
 #define LQMC_RNG_REPLAY 0    /* caller uploads the uniforms (e.g. numpy's stream)        */
 #define LQMC_RNG_PHILOX 1    /* Philox4x64-10 on the device, keyed by (seed, chain)      */
 
+/* sweep orders (dqmc mode, tiled kernel) */
+#define LQMC_ORDER_DOWN 0        /* every sweep l = L-1 .. 0, the reference's order; the right
+                                    stack of UDT factors is rebuilt at the start of each sweep */
+#define LQMC_ORDER_ALTERNATE 1   /* sweeps alternate down and up; each direction's products
+                                    serve the next sweep, so the stack is built from scratch only
+                                    after the field is set; the end-of-sweep G is at tau = 0
+                                    (down) or tau = beta (up), both equal to G(0)             */
+
 /* per-chain status bits (lqmc_get_status) */
 #define LQMC_STATUS_NONFINITE 1   /* NaN/Inf found in G                                  */
 #define LQMC_STATUS_SINGULAR 2    /* zero pivot in an LU factorisation                   */
@@ -90,7 +98,9 @@ extern "C" {
  *   [16] splitting operands of emulated float64 GEMMs, [17] their tensor-core loops
  *   (including [18]), [18] their epilogues (reading and combining the accumulators),
  *   [19] the delayed-update flushes G -= X Y^T, [20] waiting at the per-site cluster barrier.
- *   [21..23] reserved.                                                                        */
+ *   [21] alternating sweep order: 0 = no products kept (the next sweep builds them and goes
+ *   down), 1 = the next sweep goes up, 2 = the next sweep goes down; reset to 0 when the field
+ *   or the chain state is set.  [22..23] reserved.                                             */
 #define LQMC_DIAG_LEN 24
 
 typedef struct lqmc_params {
@@ -108,7 +118,11 @@ typedef struct lqmc_params {
                               keeps in native float64 (0: all on the tensor cores)            */
     int32_t measure_tau;   /* 1: measured sweeps also accumulate the unequal-time G(tau_l, 0)
                               of every slice (LQMC_MODE_DQMC only; lqmc_get_green_tau)      */
-    int32_t reserved[3];
+    int32_t sweep_order;   /* LQMC_ORDER_*; LQMC_ORDER_ALTERNATE runs every chain on the tiled
+                              kernel (LQMC_MODE_DQMC only)                                    */
+    int32_t oz_stages;     /* LQMC_PREC_FP64E: stage buffers of the emulated GEMM's copy / MMA
+                              ring, 1 .. 3 (0: two, or one where two do not fit)             */
+    int32_t reserved[1];
 } lqmc_params;
 
 /* product categories of the fp64e engine (lqmc_params.fp64e_native) */

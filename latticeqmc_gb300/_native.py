@@ -19,6 +19,7 @@ MODES = {"compat": 0, "dqmc": 1, "det": 2}
 PRECISIONS = {"fp64": 0, "mixed": 1, "fp64e": 2}
 RNGS = {"replay": 0, "philox": 1}
 ENGINES = {"auto": 0, "smem": 1, "tiled": 2}
+ORDERS = {"down": 0, "alternate": 1}
 STATUS_NONFINITE, STATUS_SINGULAR, STATUS_DRIFT, STATUS_TIMEOUT = 1, 2, 4, 8
 DEBUG_STALL_TC_WAIT = 1
 FP64E_NATIVE = {"wrap": 1, "stack": 2, "udt": 4, "green": 8, "update": 16, "lu": 32,
@@ -36,7 +37,8 @@ class Params(ctypes.Structure):
                 ("stab_every", ctypes.c_int32), ("delay", ctypes.c_int32), ("record", ctypes.c_int32),
                 ("seed", ctypes.c_uint64), ("device", ctypes.c_int32), ("engine", ctypes.c_int32),
                 ("debug", ctypes.c_int32), ("fp64e_native", ctypes.c_int32),
-                ("measure_tau", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
+                ("measure_tau", ctypes.c_int32), ("sweep_order", ctypes.c_int32),
+                ("oz_stages", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
 
 
 class LqmcError(RuntimeError):
@@ -113,7 +115,8 @@ class Handle:
     """Owns one lqmc_handle; every call checks the return code."""
 
     def __init__(self, mode, precision, rng, stab_every, delay, seed, record, device,
-                 engine="auto", debug=0, fp64e_native=("lu", "lu_rhs"), measure_tau=False):
+                 engine="auto", debug=0, fp64e_native=("lu", "lu_rhs"), measure_tau=False,
+                 sweep_order="down", oz_stages=0):
         self.lib = load()
         if isinstance(fp64e_native, int):
             native = fp64e_native
@@ -130,7 +133,9 @@ class Handle:
                    seed=int(seed) & ((1 << 64) - 1), device=int(device),
                    engine=_choice(ENGINES, engine, "engine"),
                    debug=int(debug), fp64e_native=int(native),
-                   measure_tau=int(bool(measure_tau)))
+                   measure_tau=int(bool(measure_tau)),
+                   sweep_order=_choice(ORDERS, sweep_order, "sweep order"),
+                   oz_stages=int(oz_stages))
         h = ctypes.c_void_p()
         rc = self.lib.lqmc_create(ctypes.byref(p), ctypes.byref(h))
         if rc != LQMC_OK:

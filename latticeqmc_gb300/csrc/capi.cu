@@ -22,7 +22,12 @@ cudaError_t launch_green_tau(const ChainDesc* d_descs, int n_chains, size_t smem
 size_t sweep_tiled_smem_bytes(int n, bool fp32, int delay, bool emu, int stages, bool xy_global);
 int sweep_tiled_delay_target(bool fp32, int requested, bool emu);
 int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap, bool emu, int stages);
-size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32, bool emu, int xy_delay);
+size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32, bool emu, int xy_delay, bool alt);
+size_t sweep_tiled_presplit_bytes(int n);
+cudaError_t launch_presplit(const void* d_jobs, int count, cudaStream_t stream);
+size_t sweep_tiled_presplit_job_bytes();
+void sweep_tiled_presplit_job(void* job, const double* expk, const double* expkinv,
+                              unsigned char* out, int n);
 cudaError_t launch_sweep_tiled(const ChainDesc* d_descs, int n_chains, size_t smem, int precision,
                                int n_sweeps, int measure, int sweep_base, cudaStream_t stream);
 }  // namespace lqmc
@@ -33,6 +38,7 @@ namespace {
 
 constexpr int kMaxSitesSmem = 128;    // one-CTA shared-memory kernel (both modes)
 constexpr int kMaxSitesTiled = 1024;  // tiled kernel (dqmc mode): 4 rows per thread
+constexpr int kMaxOzStages = 2;       // stage buffers of the emulated GEMM
 
 // which sweep kernel runs a chain
 enum Kind : int { kSmemFp64 = 0, kTiledFp64 = 1, kTiledFp32 = 2, kTiledFp64e = 3 };
@@ -73,6 +79,7 @@ struct lqmc_handle {
     int32_t* d_status = nullptr;
     int8_t* d_dec = nullptr;
     size_t dec_cap = 0;
+    unsigned char* d_pre = nullptr;    // split constant operands of the emulated GEMMs
     std::vector<Bucket> buckets;
     cudaEvent_t fork = nullptr;
     cudaStream_t last_stream = nullptr;
@@ -115,6 +122,8 @@ void release(lqmc_handle* h) {
     if (h->d_i8) cudaFree(h->d_i8);
     if (h->d_status) cudaFree(h->d_status);
     if (h->d_dec) cudaFree(h->d_dec);
+    if (h->d_pre) cudaFree(h->d_pre);
+    h->d_pre = nullptr;
     h->d_f64 = nullptr;
     h->d_i8 = nullptr;
     h->d_status = nullptr;
@@ -169,6 +178,14 @@ int lqmc_create(const lqmc_params* params, lqmc_handle** out) {
         return fail(nullptr, LQMC_ERR_INVALID, "measure_tau must be 0 or 1");
     if (params->measure_tau && params->mode != LQMC_MODE_DQMC)
         return fail(nullptr, LQMC_ERR_UNSUPPORTED, "the unequal-time G is measured in dqmc mode only");
+    if (params->oz_stages < 0 || params->oz_stages > kMaxOzStages)
+        return fail(nullptr, LQMC_ERR_INVALID, "oz_stages out of range");
+    if (params->sweep_order != LQMC_ORDER_DOWN && params->sweep_order != LQMC_ORDER_ALTERNATE)
+        return fail(nullptr, LQMC_ERR_INVALID, "unknown sweep order");
+    if (params->sweep_order == LQMC_ORDER_ALTERNATE && params->mode != LQMC_MODE_DQMC)
+        return fail(nullptr, LQMC_ERR_UNSUPPORTED, "the alternating sweep order is a dqmc-mode order");
+    if (params->sweep_order == LQMC_ORDER_ALTERNATE && params->engine == LQMC_ENGINE_SMEM)
+        return fail(nullptr, LQMC_ERR_UNSUPPORTED, "the alternating sweep order runs on the tiled kernel");
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess) return fail(nullptr, LQMC_ERR_CUDA, std::string("cudaGetDeviceCount: ") + cudaGetErrorString(e));
@@ -254,9 +271,10 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
         d.drift_tol = 1e-6;
         d.debug = h->p.debug;
         d.native = h->p.fp64e_native;
+        d.order = h->p.sweep_order;
         if (h->p.precision == LQMC_PREC_MIXED) kind[c] = kTiledFp32;
         else if (h->p.precision == LQMC_PREC_FP64E) kind[c] = kTiledFp64e;
-        else if (h->p.engine == LQMC_ENGINE_TILED) kind[c] = kTiledFp64;
+        else if (h->p.engine == LQMC_ENGINE_TILED || h->p.sweep_order == LQMC_ORDER_ALTERNATE) kind[c] = kTiledFp64;
         else kind[c] = (n <= kMaxSitesSmem) ? kSmemFp64 : kTiledFp64;
         if (kind[c] == kSmemFp64 && h->p.engine == LQMC_ENGINE_SMEM && n > kMaxSitesSmem) {
             release(h);
@@ -289,8 +307,25 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
             } else if (emu && lqmc::sweep_tiled_delay(n, f32, h->p.delay, smem_cap, emu, 2) >= d.delay) {
                 d.oz_stages = 2;
             }
+            // a requested stage count: fewer always fit; more may need the delayed-update
+            // buffers moved to global memory
+            const int want = h->p.oz_stages;
+            if (emu && want > 0 && want <= d.oz_stages) d.oz_stages = want;
+            if (emu && want > d.oz_stages) {
+                if (!xy_global && lqmc::sweep_tiled_smem_bytes(n, f32, d.delay, emu, want, false) > smem_cap) {
+                    xy_global = true;
+                    d.delay = target;
+                    d.flags |= lqmc::kUpdatesInGlobal;
+                }
+                d.oz_stages = want;
+                if (lqmc::sweep_tiled_smem_bytes(n, f32, d.delay, emu, want, xy_global) > smem_cap) {
+                    release(h);
+                    return fail(h, LQMC_ERR_UNSUPPORTED, "the requested stage buffers do not fit in shared memory");
+                }
+            }
             smem[c] = lqmc::sweep_tiled_smem_bytes(n, f32, d.delay, emu, d.oz_stages, xy_global);
-            work = (lqmc::sweep_tiled_work_bytes(n, d.n_chunks, f32, emu, xy_global ? d.delay : 0) + 7) / 8;
+            work = (lqmc::sweep_tiled_work_bytes(n, d.n_chunks, f32, emu, xy_global ? d.delay : 0,
+                                                 d.order == LQMC_ORDER_ALTERNATE) + 7) / 8;
             if (smem[c] > smem_cap) { release(h); return fail(h, LQMC_ERR_UNSUPPORTED, "lattice too large for shared memory"); }
         }
         const size_t fcopy = (kind[c] == kTiledFp32) ? 2 * round_up((nn + 1) / 2, kAlign) : 0;
@@ -383,6 +418,55 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
         d.expkinv_f = ekif;
     }
 
+    // the emulated-GEMM chains' constant operands, split once and shared by every chain with
+    // the same e^{-dtau K} and e^{+dtau K} (the same lattice and dtau)
+    {
+        std::vector<int> leader(n_chains, -1);
+        std::vector<int> groups_of;   // leader chain of each group
+        for (int c = 0; c < n_chains; ++c) {
+            if (kind[c] != kTiledFp64e) continue;
+            const size_t nn = (size_t)n_sites[c] * n_sites[c];
+            for (int g : groups_of) {
+                if (n_sites[g] == n_sites[c] && !std::memcmp(exp_k[g], exp_k[c], nn * sizeof(double)) &&
+                    !std::memcmp(exp_k_inv[g], exp_k_inv[c], nn * sizeof(double))) {
+                    leader[c] = g;
+                    break;
+                }
+            }
+            if (leader[c] < 0) {
+                leader[c] = c;
+                groups_of.push_back(c);
+            }
+        }
+        if (!groups_of.empty()) {
+            std::map<int, size_t> pre_off;
+            size_t pre_total = 0;
+            for (int g : groups_of) {
+                pre_off[g] = pre_total;
+                pre_total += round_up(lqmc::sweep_tiled_presplit_bytes(n_sites[g]), 256);
+            }
+            e = cudaMalloc(&h->d_pre, pre_total);
+            if (e != cudaSuccess) { release(h); return fail(h, LQMC_ERR_NOMEM, "device allocation of the split constants failed"); }
+            const size_t jb = lqmc::sweep_tiled_presplit_job_bytes();
+            std::vector<unsigned char> jobs(jb * groups_of.size());
+            for (size_t k = 0; k < groups_of.size(); ++k) {
+                const int g = groups_of[k];
+                lqmc::sweep_tiled_presplit_job(jobs.data() + k * jb, h->desc[g].expk, h->desc[g].expkinv,
+                                               h->d_pre + pre_off[g], n_sites[g]);
+            }
+            void* d_jobs = nullptr;
+            e = cudaMalloc(&d_jobs, jobs.size());
+            if (e != cudaSuccess) { release(h); return fail(h, LQMC_ERR_NOMEM, "presplit job allocation failed"); }
+            e = cudaMemcpy(d_jobs, jobs.data(), jobs.size(), cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) e = lqmc::launch_presplit(d_jobs, (int)groups_of.size(), nullptr);
+            if (e == cudaSuccess) e = cudaDeviceSynchronize();
+            cudaFree(d_jobs);
+            if (e != cudaSuccess) { release(h); return cuda_fail(h, e, "splitting the constant operands"); }
+            for (int c = 0; c < n_chains; ++c)
+                if (leader[c] >= 0) h->desc[c].presplit = h->d_pre + pre_off[leader[c]];
+        }
+    }
+
     // buckets of equal shared-memory footprint, largest first
     // buckets of one kernel and one shared-memory footprint; the largest lattices first
     std::map<std::pair<int, size_t>, std::vector<int>> groups;
@@ -421,6 +505,8 @@ int lqmc_set_field(lqmc_handle* h, int32_t chain, const int8_t* field) {
         if (r) return r;
     }
     LQMC_CK(h, cudaMemcpy(d.field, t.data(), t.size(), cudaMemcpyHostToDevice));
+    // a new field invalidates the products the alternating order keeps between sweeps
+    LQMC_CK(h, cudaMemset(d.diag + 21, 0, sizeof(double)));
     h->field_set[chain] = 1;
     return LQMC_OK;
 }
@@ -666,6 +752,8 @@ int lqmc_set_chain_state(lqmc_handle* h, int32_t chain, const double* diag, cons
         if (!(diag[7] >= 0.0) || diag[7] != (double)(int64_t)diag[7])
             return fail(h, LQMC_ERR_INVALID, "diagnostics[7] (sweep counter) must be a non-negative integer");
         LQMC_CK(h, cudaMemcpy(d.diag, diag, LQMC_DIAG_LEN * sizeof(double), cudaMemcpyHostToDevice));
+        // the kept products are not part of a checkpoint: the next sweep rebuilds them
+        LQMC_CK(h, cudaMemset(d.diag + 21, 0, sizeof(double)));
     }
     if (green_sum)
         LQMC_CK(h, cudaMemcpy(d.gsum, green_sum, 2 * (size_t)d.n * d.n * sizeof(double), cudaMemcpyHostToDevice));

@@ -50,6 +50,10 @@ struct ChainDesc {
     double* tau_work;         // per spin: (n_chunks + 1) UDT slots, then X (+ scratch)
     int32_t tau_flags;        // kScratchInGlobal: the G(tau) kernel's two scratch matrices
     int32_t tau_pad;
+    const unsigned char* presplit;   // emulated-GEMM kernel: the split constant operands,
+                                     // shared by the chains with the same e^{-dtau K}
+    int32_t order;            // LQMC_ORDER_* (tiled kernel)
+    int32_t order_pad;
 };
 
 }  // namespace lqmc

@@ -55,10 +55,12 @@ constexpr int kTmemCols = kSlices * kBN;      // 512: the whole tensor memory of
 constexpr int kNonFinite = 1 << 20;
 
 // The epilogue drops the 12 low bits of the combined diagonals (so that the sum fits int64).
-// 0: floor them (a one-signed error below 2^-49 of 2^(E_i + F_j)); 1: round them to nearest
-// (half that, no bias).  The default is the measured configuration.
+// 1 (default): round them to nearest (an error below 2^-50 of 2^(E_i + F_j), either sign, no
+// bias); 0: floor them (below 2^-49, one-signed).  At 16x16, beta=8, stabilisation every 8
+// slices, rounding lowered the fp64e engine's median stabilisation residual about 3x and its
+// G error against float64 2-3x (16 chains, 6 sweeps).
 #ifndef LQMC_OZ_ROUND_EPILOGUE
-#define LQMC_OZ_ROUND_EPILOGUE 0
+#define LQMC_OZ_ROUND_EPILOGUE 1
 #endif
 constexpr long long kLowRound = LQMC_OZ_ROUND_EPILOGUE ? (1ll << 11) : 0;
 constexpr long long kWaitCycles = 2000000000ll;   // ~1 s of SM clock before a wait gives up
@@ -183,42 +185,68 @@ __device__ __forceinline__ long long fixed55(double v, int e, int off) {
     return bits < 0 ? -(long long)mag : (long long)mag;
 }
 
+// Scratch offsets (ints) in the stage buffer: the exponent maxima of split_tiles (rows <=
+// 1024), the k-scaling shifts, and the per-stripe maxima of a transposed split (<= kNT * 8).
+constexpr int kMaxKscale = 1024;
+constexpr int kScratchKA = 2048, kScratchKB = kScratchKA + kMaxKscale;
+constexpr int kScratchStripes = kScratchKB + kMaxKscale;
+static_assert((kScratchStripes + 8 * kNT) * sizeof(int) <= (kStepA + kStepB) * sizeof(__nv_bfloat16),
+              "split scratch fits one stage buffer");
+
 // Split X (rows x k), X(r, q) = trans ? x[q ld + r] : x[r ld + q], into the tile layout with
 // row blocks of BLK rows: slice t of (row block rb, k step s) at
 // ((rb * S + s) * kSlices + t) * BLK * kBK, S = kpad(k) / kBK.  Rows >= `rows` and k >= `k`
-// are zero.  exps[r] = E_r.  `scratch` is shared memory of at least rows ints.
+// are zero.  exps[r] = E_r.  `scratch` is shared memory of kScratchStripes + 8 kNT ints.
 //
-// Both passes read 8 consecutive elements of memory per unit with independent loads, so
-// many L2 requests are in flight: the row maxima of the biased exponents are gathered with
-// shared-memory atomics (an exponent of 0x7FF, NaN or Inf, dominates and marks the row).
+// The exponent pass keeps its maxima in registers and reduces them per warp (row-contiguous
+// X) or through one shared-memory combine of per-stripe maxima (transposed X), without
+// atomics; NaN or Inf (biased exponent 0x7FF) dominates and marks the row.  The digit pass
+// reads 8 consecutive elements of memory per unit with independent loads, so many L2
+// requests are in flight.
 // kshift (optional, k ints): element (r, q) is split as X(r, q) 2^kshift[q] (exact).
 template <int BLK>
 __device__ void split_tiles(const double* x, int ld, bool trans, int rows, int k, int* exps,
                             __nv_bfloat16* dst, int* scratch, const int* kshift = nullptr) {
     const int kp = kpad(k), S = kp / kBK, rp = rows_pad(rows, BLK);
-    for (int r = threadIdx.x; r < rows; r += kNT) scratch[r] = 0;
-    __syncthreads();
     if (!trans) {
-        // unit (r, q8): x[r ld + 8 q8 ..]
-        const int g8 = (k + 7) / 8;
-        for (int u = threadIdx.x; u < rows * g8; u += kNT) {
-            const int r = u / g8, q0 = (u % g8) * 8;
+        // one warp per row: lanes read 8 consecutive k each (a warp covers 256 contiguous
+        // elements), then one warp max-reduction
+        const int lane = lane_id();
+        for (int r = warp_id(); r < rows; r += kNW) {
             int emax = 0;
+            for (int q0 = 8 * lane; q0 < k; q0 += 256) {
 #pragma unroll
-            for (int c = 0; c < 8; ++c)
-                if (q0 + c < k)
-                    emax = max(emax, biased_exp(x[(size_t)r * ld + q0 + c], kshift ? kshift[q0 + c] : 0));
-            atomicMax(&scratch[r], emax);
+                for (int c = 0; c < 8; ++c)
+                    if (q0 + c < k)
+                        emax = max(emax, biased_exp(x[(size_t)r * ld + q0 + c], kshift ? kshift[q0 + c] : 0));
+            }
+            emax = __reduce_max_sync(0xffffffffu, emax);
+            if (lane == 0) scratch[r] = emax;
         }
     } else {
-        // unit (q, r8): x[q ld + 8 r8 ..], eight rows
-        const int g8 = (rows + 7) / 8;
-        for (int u = threadIdx.x; u < k * g8; u += kNT) {
-            const int q = u / g8, r0 = (u % g8) * 8;
-            const int off = kshift ? kshift[q] : 0;
+        // thread (group of 8 consecutive rows, stripe of k) keeps 8 maxima in registers while
+        // it walks its stripe (a warp, 32 groups of one k, reads contiguous memory); the
+        // stripes' maxima are combined through shared memory
+        int* part = scratch + kScratchStripes;
+        const int g8 = (rows + 7) / 8, nq = max(1, kNT / g8);
+        if (threadIdx.x < g8 * nq) {
+            const int r0 = (threadIdx.x % g8) * 8, qs = threadIdx.x / g8;
+            int em[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int q = qs; q < k; q += nq) {
+                const int off = kshift ? kshift[q] : 0;
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    if (r0 + c < rows) em[c] = max(em[c], biased_exp(x[(size_t)q * ld + r0 + c], off));
+            }
 #pragma unroll
             for (int c = 0; c < 8; ++c)
-                if (r0 + c < rows) atomicMax(&scratch[r0 + c], biased_exp(x[(size_t)q * ld + r0 + c], off));
+                if (r0 + c < rows) part[qs * rows + r0 + c] = em[c];
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < rows; r += kNT) {
+            int emax = 0;
+            for (int qs = 0; qs < nq; ++qs) emax = max(emax, part[qs * rows + r]);
+            scratch[r] = emax;
         }
     }
     __syncthreads();
@@ -270,9 +298,7 @@ __device__ void split_tiles(const double* x, int ld, bool trans, int rows, int k
     }
 }
 
-// Scratch offsets (ints) of the k-scaling shifts, after the exponent maxima of split_tiles.
-constexpr int kMaxKscale = 1024;
-constexpr int kScratchKA = 2048, kScratchKB = kScratchKA + kMaxKscale;
+
 
 // out[q] = largest biased exponent (zero and non-finite entries excluded) of X(:, q),
 // X(r, q) = trans ? x[q ld + r] : x[r ld + q], r < rows, q < k

@@ -28,12 +28,24 @@ __host__ __device__ __forceinline__ void philox4x64_10(uint64_t c[4], uint64_t k
     }
 }
 
+// (word >> 11) 2^-53: a uniform on [0, 1) with 53 random bits
+__host__ __device__ __forceinline__ double philox_to_unit(uint64_t w) {
+    return (double)(w >> 11) * (1.0 / 9007199254740992.0);
+}
+
+// The four uniforms of positions 4 q .. 4 q + 3 of sweep t: one Philox call
+__host__ __device__ __forceinline__ void philox_uniform4(uint64_t seed, uint64_t chain,
+                                                         uint64_t sweep, uint64_t q, double u[4]) {
+    uint64_t c[4] = {q, sweep, 0ull, 0ull};
+    philox4x64_10(c, seed, chain);
+    for (int w = 0; w < 4; ++w) u[w] = philox_to_unit(c[w]);
+}
+
 __host__ __device__ __forceinline__ double philox_uniform(uint64_t seed, uint64_t chain,
                                                           uint64_t sweep, uint64_t pos) {
     uint64_t c[4] = {pos >> 2, sweep, 0ull, 0ull};
     philox4x64_10(c, seed, chain);
-    const uint64_t w = c[pos & 3];
-    return (double)(w >> 11) * (1.0 / 9007199254740992.0);
+    return philox_to_unit(c[pos & 3]);
 }
 
 }  // namespace lqmc

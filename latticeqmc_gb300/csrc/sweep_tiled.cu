@@ -42,9 +42,29 @@ int sweep_tiled_delay(int n, bool fp32, int requested, size_t cap, bool emu, int
     return k;
 }
 
-size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32, bool emu, int xy_delay) {
-    return fp32 ? TiledLayout<float>(n, n_chunks, false, xy_delay).total
-                : TiledLayout<double>(n, n_chunks, emu, xy_delay).total;
+size_t sweep_tiled_work_bytes(int n, int n_chunks, bool fp32, bool emu, int xy_delay, bool alt) {
+    return fp32 ? TiledLayout<float>(n, n_chunks, false, xy_delay, alt).total
+                : TiledLayout<double>(n, n_chunks, emu, xy_delay, alt).total;
+}
+
+size_t sweep_tiled_presplit_bytes(int n) { return PresplitLayout(n).total; }
+
+// split the constant operands of `count` jobs (device array) on `stream`
+cudaError_t launch_presplit(const void* d_jobs, int count, cudaStream_t stream) {
+    if (count <= 0) return cudaSuccess;
+    presplit_kernel<<<kNumPre * count, kNT, 0, stream>>>(static_cast<const PresplitJob*>(d_jobs));
+    return cudaGetLastError();
+}
+
+size_t sweep_tiled_presplit_job_bytes() { return sizeof(PresplitJob); }
+
+void sweep_tiled_presplit_job(void* job, const double* expk, const double* expkinv,
+                              unsigned char* out, int n) {
+    PresplitJob* j = static_cast<PresplitJob*>(job);
+    j->expk = expk;
+    j->expkinv = expkinv;
+    j->out = out;
+    j->n = n;
 }
 
 // precision: 0 float64, 1 float32 (mixed), 2 float64 with emulated tensor-core GEMMs

@@ -43,9 +43,12 @@ __host__ __device__ constexpr size_t align256(size_t b) { return (b + 255) / 256
 // the UDT slots of both spins.
 template <typename T>
 struct TiledLayout {
-    size_t nn, g, z, s, oz, oz_ea, xy, spin_block, slot, total, g_slots, pre, pre_a, pre_b, pre_e;
-    // xy_delay > 0: the spin blocks also hold the delayed-update buffers X, Y (n x (k + 1))
-    __host__ __device__ TiledLayout(int n, int n_chunks, bool emu = false, int xy_delay = 0) {
+    size_t nn, g, z, s, oz, oz_ea, xy, spin_block, slot, total, g_slots;
+    // xy_delay > 0: the spin blocks also hold the delayed-update buffers X, Y (n x (k + 1));
+    // alt: the alternating sweep order keeps a left product at every chunk boundary (n_chunks
+    // slots per spin) instead of a ping-pong pair
+    __host__ __device__ TiledLayout(int n, int n_chunks, bool emu = false, int xy_delay = 0,
+                                    bool alt = false) {
         nn = (size_t)n * n;
         g = 0;                                              // G of the spin       (T)
         z = g + align256(nn * sizeof(T));                   // Z0, Z1 GEMM temps   (T)
@@ -58,14 +61,26 @@ struct TiledLayout {
         spin_block = xy + (xy_delay > 0 ? align256(2 * (size_t)n * (xy_delay + 1) * sizeof(T)) : 0);
         g_slots = 2 * spin_block;
         slot = align256(2 * nn * sizeof(T) + (size_t)(n + 1) * sizeof(double));
-        pre = g_slots + (size_t)(2 * n_chunks + 4) * slot;
-        // emulated GEMMs: e^{-dtau K} (as A, and transposed as A), e^{+dtau K} (as A) and
-        // e^{-dtau K} (as B) split once per launch, shared by the chain's two CTAs
-        pre_a = emu ? align256((size_t)ozt::kSlices * ozt::rows_pad(n, ozt::kBM) * ozt::kpad(n) * 2) : 0;
-        pre_b = emu ? align256((size_t)ozt::kSlices * ozt::rows_pad(n, ozt::kBN) * ozt::kpad(n) * 2) : 0;
-        pre_e = pre + 3 * pre_a + pre_b;
-        total = pre_e + (emu ? align256(4 * (size_t)n * sizeof(int)) : 0);
+        const int n_slots = alt ? (4 * n_chunks > 2 * n_chunks + 4 ? 4 * n_chunks : 2 * n_chunks + 4)
+                                : 2 * n_chunks + 4;
+        total = g_slots + (size_t)n_slots * slot;
     }
+};
+
+// The constant operands of the emulated GEMMs, split once per handle and shared by every
+// chain with the same e^{-dtau K} and e^{+dtau K}: e^{-dtau K} as A, its transpose as A,
+// e^{+dtau K} as A (row blocks of kBM), e^{-dtau K} as B and e^{+dtau K} as B (column blocks of
+// kBN), then the five exponent vectors (n ints each).  Byte offsets from the region's start.
+struct PresplitLayout {
+    size_t a, b, e, total;
+    __host__ __device__ PresplitLayout(int n) {
+        a = align256((size_t)ozt::kSlices * ozt::rows_pad(n, ozt::kBM) * ozt::kpad(n) * 2);
+        b = align256((size_t)ozt::kSlices * ozt::rows_pad(n, ozt::kBN) * ozt::kpad(n) * 2);
+        e = 3 * a + 2 * b;
+        total = e + align256(5 * (size_t)n * sizeof(int));
+    }
+    // operands 0..2 are A operands (a bytes each), 3..4 B operands (b bytes each)
+    __host__ __device__ size_t slices(int i) const { return i < 3 ? (size_t)i * a : 3 * a + (size_t)(i - 3) * b; }
 };
 
 template <typename T>
@@ -104,11 +119,11 @@ struct TSmem {
     int* piv;         // [kPanel] panel pivots
     double* stage64;  // float64 GEMM staging of the LU (float kernel; same region as stage)
     int native;       // LQMC_FP64E_NATIVE_* categories kept in native float64 (EMU kernel)
-    ozt::Presplit pre[4];   // EMU: e^{-dtau K} as A, its transpose as A, e^{+dtau K} as A,
-                            // e^{-dtau K} as B (indices kPreK, kPreKT, kPreKinv, kPreKB)
+    ozt::Presplit pre[5];   // EMU: e^{-dtau K} as A, its transpose as A, e^{+dtau K} as A,
+                            // e^{-dtau K} as B, e^{+dtau K} as B (indices kPreK .. kPreKinvB)
 };
 
-enum { kPreK = 0, kPreKT = 1, kPreKinv = 2, kPreKB = 3 };
+enum { kPreK = 0, kPreKT = 1, kPreKinv = 2, kPreKB = 3, kPreKinvB = 4, kNumPre = 5 };
 
 template <typename T> __device__ __forceinline__ T* slot_U(const TSmem<T>& sm, int idx, size_t nn) {
     return reinterpret_cast<T*>(sm.slots + (size_t)idx * sm.slot_bytes);
@@ -653,56 +668,67 @@ __device__ double green_udt_t(const ChainDesc& d, TSmem<T>& sm, const T* ur, con
     return res;
 }
 
+// UDT of the right product through chunk c, R_c = B_{hi-1} ... B_lo R_{c-1} (slices lo..hi-1
+// of the chunk), R_{c-1} from slot `in` (-1: identity), into slot `out`.
 template <typename T, bool EMU>
-__device__ void right_stack_t(const ChainDesc& d, TSmem<T>& sm, int s, double* logdet, double* sgn,
-                              int* singular) {
+__device__ void right_chunk_t(const ChainDesc& d, TSmem<T>& sm, int s, int c, int in, int out) {
     const int n = d.n, sigma = s ? -1 : 1;
     const size_t nn = (size_t)n * n;
     const T* ek = mat_expk<T>(d);
-    for (int c = 0; c < d.n_chunks; ++c) {
-        const int lo = c * d.stab_every, hi = min(lo + d.stab_every, d.L);
-        const int prev = s * d.n_chunks + c - 1, cur = s * d.n_chunks + c;
-        T* za = sm.z0;
-        T* zb = sm.z1;
-        for (int l = lo; l < hi; ++l) {
-            load_ev_t<T>(d, sm, l, sigma);
-            __syncthreads();
-            GemmOpt<T> o;
-            o.rs = sm.ev_t;
-            if (l == lo && c == 0) {
-                // e^V e^{-dtau K}: the first factor itself
-                for (int i = warp_id(); i < n; i += kNW)
-                    for (int j = lane_id(); j < n; j += 32)
-                        zb[(size_t)i * n + j] = sm.ev_t[i] * ek[(size_t)i * n + j];
-                __syncthreads();
-            } else if (l == lo) {
-                // B(p, j) = U[p][j] = uc[j n + p] (column-major slot)
-                gemm_t<T, EMU, LQMC_FP64E_NATIVE_STACK, false, true>(sm, zb, n, ek, n, slot_U(sm, prev, nn), n, n, n, n, o,
-                                                                     kPreK);
-            } else {
-                // e^V e^{-dtau K} Z
-                gemm_t<T, EMU, LQMC_FP64E_NATIVE_STACK, false, false>(sm, zb, n, ek, n, za, n, n, n, n, o, kPreK);
-            }
-            T* t = za; za = zb; zb = t;
-        }
-        const double sg = udt_absorb_t<T, EMU>(d, sm, za, c ? slot_d(sm, prev, nn) : nullptr,
-                                          c ? slot_T(sm, prev, nn) : nullptr, slot_U(sm, cur, nn),
-                                          slot_d(sm, cur, nn), slot_T(sm, cur, nn));
-        if (threadIdx.x == 0) slot_d(sm, cur, nn)[n] = sg;
+    const int lo = c * d.stab_every, hi = min(lo + d.stab_every, d.L);
+    const int lane = lane_id();
+    T* za = sm.z0;
+    T* zb = sm.z1;
+    for (int l = lo; l < hi; ++l) {
+        load_ev_t<T>(d, sm, l, sigma);
         __syncthreads();
+        GemmOpt<T> o;
+        o.rs = sm.ev_t;
+        if (l == lo && in < 0) {
+            // e^V e^{-dtau K}: the first factor itself
+            for (int i = warp_id(); i < n; i += kNW)
+                for (int j = lane; j < n; j += 32)
+                    zb[(size_t)i * n + j] = sm.ev_t[i] * ek[(size_t)i * n + j];
+            __syncthreads();
+        } else if (l == lo) {
+            // B(p, j) = U[p][j] = uc[j n + p] (column-major slot)
+            gemm_t<T, EMU, LQMC_FP64E_NATIVE_STACK, false, true>(sm, zb, n, ek, n, slot_U(sm, in, nn), n, n, n, n, o,
+                                                                 kPreK);
+        } else {
+            // e^V e^{-dtau K} Z
+            gemm_t<T, EMU, LQMC_FP64E_NATIVE_STACK, false, false>(sm, zb, n, ek, n, za, n, n, n, n, o, kPreK);
+        }
+        T* t = za; za = zb; zb = t;
     }
+    const double sg = udt_absorb_t<T, EMU>(d, sm, za, in >= 0 ? slot_d(sm, in, nn) : nullptr,
+                                      in >= 0 ? slot_T(sm, in, nn) : nullptr, slot_U(sm, out, nn),
+                                      slot_d(sm, out, nn), slot_T(sm, out, nn));
+    if (threadIdx.x == 0) slot_d(sm, out, nn)[n] = sg;
+    __syncthreads();
+}
+
+// Right stack R_0 .. R_{K-1} of spin s from scratch (slots s K + c) and G = (1 + R_{K-1})^-1.
+template <typename T, bool EMU>
+__device__ void right_stack_t(const ChainDesc& d, TSmem<T>& sm, int s, double* logdet, double* sgn,
+                              int* singular) {
+    const int n = d.n;
+    const size_t nn = (size_t)n * n;
+    for (int c = 0; c < d.n_chunks; ++c)
+        right_chunk_t<T, EMU>(d, sm, s, c, c ? s * d.n_chunks + c - 1 : -1, s * d.n_chunks + c);
     const int top = s * d.n_chunks + d.n_chunks - 1;
     green_udt_t<T, EMU>(d, sm, slot_U(sm, top, nn), slot_d(sm, top, nn), slot_T(sm, top, nn),
                    slot_d(sm, top, nn)[n], nullptr, nullptr, nullptr, 1.0, sm.g, false, logdet,
                    sgn, singular);
 }
 
+// UDT of the transposed left product through slices lo..hi-1, C^T = B_lo^T ... B_{hi-1}^T L_in
+// (L_in from slot `in`; -1: identity), into slot `out`.
 template <typename T, bool EMU>
-__device__ void left_step_t(const ChainDesc& d, TSmem<T>& sm, int s, int p_in, bool first, int lo,
+__device__ void left_step_t(const ChainDesc& d, TSmem<T>& sm, int s, int in, int out, int lo,
                             int hi) {
     const int n = d.n, sigma = s ? -1 : 1;
     const size_t nn = (size_t)n * n;
-    const int in = 2 * d.n_chunks + 2 * s + p_in, out = 2 * d.n_chunks + 2 * s + (1 - p_in);
+    const bool first = in < 0;
     const T* ek = mat_expk<T>(d);
     T* za = sm.z0;
     T* zb = sm.z1;
@@ -712,7 +738,7 @@ __device__ void left_step_t(const ChainDesc& d, TSmem<T>& sm, int s, int p_in, b
         __syncthreads();
         if (l == hi - 1) {
             // za = e^V U (U column-major in the slot; identity on the first chunk)
-            const T* u = slot_U(sm, in, nn);
+            const T* u = first ? nullptr : slot_U(sm, in, nn);
             for (int k = warp_id(); k < n; k += kNW)
                 for (int i = lane; i < n; i += 32)
                     za[(size_t)i * n + k] = first ? (i == k ? sm.ev_t[i] : T(0))
@@ -733,58 +759,121 @@ __device__ void left_step_t(const ChainDesc& d, TSmem<T>& sm, int s, int p_in, b
     __syncthreads();
 }
 
+// Wrap across slice l.  Down (from slice l to l - 1): G <- B_l^-1 G B_l =
+// e^{+dtau K} e^{-V_l} G e^{V_l} e^{-dtau K}.  Up (from slice l - 1 to l, the alternating
+// order's upward sweep): G <- B_l G B_l^-1 = e^{V_l} e^{-dtau K} G e^{+dtau K} e^{-V_l}.  Both
+// directions share the two product call sites; not inlined into the kernel.
 template <typename T, bool EMU>
-__device__ void wrap_t(const ChainDesc& d, TSmem<T>& sm, int l) {
+__device__ __noinline__ void wrap_t(const ChainDesc& d, TSmem<T>& sm, int l, bool up = false) {
     const int n = d.n;
     load_ev_t<T>(d, sm, l, sm.spin ? -1 : 1);
     __syncthreads();
     T* g = sm.g;
-    for (int i = warp_id(); i < n; i += kNW)
-        for (int j = lane_id(); j < n; j += 32) g[(size_t)i * n + j] *= sm.iev_t[i];
-    GemmOpt<T> o;
-    o.cs = sm.ev_t;
-    gemm_t<T, EMU, LQMC_FP64E_NATIVE_WRAP, false, false>(sm, sm.z0, n, mat_expkinv<T>(d), n, g, n, n, n, n, o,
-                                                         kPreKinv);
-    gemm_t<T, EMU, LQMC_FP64E_NATIVE_WRAP, false, false>(sm, g, n, sm.z0, n, mat_expk<T>(d), n, n, n, n,
-                                                         GemmOpt<T>(), -1, kPreKB);
+    GemmOpt<T> o1, o2;
+    if (up) {
+        o1.rs = sm.ev_t;
+        o2.cs = sm.iev_t;
+    } else {
+        for (int i = warp_id(); i < n; i += kNW)
+            for (int j = lane_id(); j < n; j += 32) g[(size_t)i * n + j] *= sm.iev_t[i];
+        o1.cs = sm.ev_t;
+    }
+    gemm_t<T, EMU, LQMC_FP64E_NATIVE_WRAP, false, false>(sm, sm.z0, n, up ? mat_expk<T>(d) : mat_expkinv<T>(d),
+                                                         n, g, n, n, n, n, o1, up ? kPreK : kPreKinv);
+    gemm_t<T, EMU, LQMC_FP64E_NATIVE_WRAP, false, false>(sm, g, n, sm.z0, n, up ? mat_expkinv<T>(d) : mat_expk<T>(d),
+                                                         n, n, n, n, o2, -1, up ? kPreKinvB : kPreKB);
 }
 
-// Site updates of slice l with delayed rank-k updates (k = d.delay): the accepted flips of
-// the slice accumulate as G_eff = G - X Y^T with x = G_eff[:, i], y = (D/R)(e_i - G_eff[i, :])
-// (the Sherman-Morrison update of lqmc.py:318-331 with the defects fixed); every k flips,
-// and at the end of the slice, G -= X Y^T as one tiled GEMM per spin.
+// G <- G^T in place (through Z0)
+template <typename T>
+__device__ void transpose_green(TSmem<T>& sm, int n) {
+    for (int i = warp_id(); i < n; i += kNW)
+        for (int j = lane_id(); j < n; j += 32) sm.z0[(size_t)j * n + i] = sm.g[(size_t)i * n + j];
+    __syncthreads();
+    for (size_t e = threadIdx.x; e < (size_t)n * n; e += kNT) sm.g[e] = sm.z0[e];
+    __syncthreads();
+}
+
+// One element global -> shared through the asynchronous copy unit (cp.async; completes on
+// this thread's async_copy_wait_all).
+template <typename T>
+__device__ __forceinline__ void async_copy_elem(T* dst_smem, const T* src) {
+    static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n"
+                 :: "r"((unsigned)__cvta_generic_to_shared(dst_smem)), "l"(src), "n"(sizeof(T))
+                 : "memory");
+}
+__device__ __forceinline__ void async_copy_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void async_copy_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// Site updates of slice l, visited as step `step` of the sweep (the index of its uniforms and
+// decisions: L - 1 - l going down, l going up), with delayed rank-k updates (k = d.delay): the
+// accepted flips of the slice accumulate as G_eff = G - X Y^T with x = G_eff[:, i],
+// y = (D/R)(e_i - G_eff[i, :]) (the Sherman-Morrison update of lqmc.py:318-331 with the defects
+// fixed); every k flips, and at the end of the slice, G -= X Y^T as one GEMM per spin.
+//
+// The per-site critical path (ratio, cluster exchange, acceptance) reads only shared memory:
+// the slice's uniforms (one Philox call per four sites, in parallel), its field values and
+// G's diagonal are staged before the sites are visited (the diagonal again after every flush),
+// and the row and column of G of site i + 1 are copied asynchronously while site i is decided.
 template <typename T, bool EMU>
-__device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int sw, uint64_t sweep_id,
-                               int* accepted) {
+__device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int step, int sw,
+                               uint64_t sweep_id, int* accepted) {
     namespace cg = cooperative_groups;
     cg::cluster_group cluster = cg::this_cluster();
-    const int n = d.n, L = d.L, step = L - 1 - l, kd = d.delay, ld = kd + 1, sp = sm.spin;
+    const int n = d.n, L = d.L, kd = d.delay, ld = kd + 1, sp = sm.spin;
     T* g = sm.g;
     int8_t* f = d.field + (size_t)l * n;
+    // staging buffers, free while sites are updated (they serve the QR otherwise)
+    double* uni = sm.nrm;      // [n] the slice's uniforms
+    double* gdiag = sm.tau;    // [n] diag(G) of this spin
+    int* fv = sm.order;        // [n] the slice's field values at its start
+    T* cnext = sm.xt[1];       // [n] G[:, i + 1]
+    T* rnext = sm.yt[1];       // [n] G[i + 1, :]
+    {
+        const size_t base = (size_t)step * n;
+        if (d.rng == LQMC_RNG_REPLAY) {
+            for (int i = threadIdx.x; i < n; i += kNT) uni[i] = d.uniforms[(size_t)sw * n * L + base + i];
+        } else {
+            const uint64_t q0 = base >> 2, q1 = (base + n - 1) >> 2;
+            for (uint64_t q = q0 + threadIdx.x; q <= q1; q += kNT) {
+                double u4[4];
+                philox_uniform4(d.seed, (uint64_t)d.chain_id, sweep_id, q, u4);
+#pragma unroll
+                for (int w = 0; w < 4; ++w) {
+                    const long long i = (long long)(4 * q + w) - (long long)base;
+                    if (i >= 0 && i < n) uni[i] = u4[w];
+                }
+            }
+        }
+        for (int i = threadIdx.x; i < n; i += kNT) {
+            fv[i] = f[i];
+            gdiag[i] = (double)g[(size_t)i * n + i];
+        }
+        __syncthreads();
+    }
     int m = 0;   // pending updates
     constexpr int kPer = 4;   // rows per thread: n <= kPer * kNT
-    for (int i = 0; i < n; ++i) {
-        // G[:, i] and G[i, :] of this spin, loaded before they are needed
-        T colv[kPer], rowv[kPer];
+    T colv[kPer], rowv[kPer];   // G[:, i] and G[i, :] of this spin for the site being decided
 #pragma unroll
-        for (int q = 0; q < kPer; ++q) {
-            const int j = threadIdx.x + q * kNT;
-            colv[q] = (j < n) ? g[(size_t)j * n + i] : T(0);
-            rowv[q] = (j < n) ? g[(size_t)i * n + j] : T(0);
-        }
-        // read the field before the barrier: after it either CTA may flip it
-        const int8_t s_il = f[i];
+    for (int q = 0; q < kPer; ++q) {
+        const int j = threadIdx.x + q * kNT;
+        colv[q] = (j < n) ? g[(size_t)j * n] : T(0);
+        rowv[q] = (j < n) ? g[j] : T(0);
+    }
+    for (int i = 0; i < n; ++i) {
+        const int s_il = fv[i];
         const int par = 2 * (i & 1);
         if (warp_id() == 0) {
-            // this spin's factor R_sigma = 1 + D_sigma (1 - G_eff,ii), its update coefficient
-            // D_sigma / R_sigma and the site's uniform, once per CTA; the factors are exchanged
+            // this spin's factor R_sigma = 1 + D_sigma (1 - G_eff,ii) and its update
+            // coefficient D_sigma / R_sigma, once per CTA; the factors are exchanged
             const int lane = lane_id();
             T part = T(0);
             for (int q = lane; q < m; q += 32) part = fma(sm.dx[(size_t)i * ld + q], sm.dy[(size_t)i * ld + q], part);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
             if (lane == 0) {
-                const double gv = (double)(g[(size_t)i * n + i] - part);
+                const double gv = (double)((T)gdiag[i] - part);
                 const double ep = s_il > 0 ? d.c[0] : d.c[1];
                 const double em = s_il > 0 ? d.c[1] : d.c[0];
                 const double dl = (sp ? em : ep) - 1.0;
@@ -792,44 +881,74 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int sw, 
                 sm.gii[par + sp] = r;
                 sm.peer_gii[par + sp] = r;
                 sm.gii[4 + (i & 1)] = dl / r;
-                const int pos = step * n + i;
-                sm.gii[6 + (i & 1)] = (d.rng == LQMC_RNG_REPLAY)
-                                          ? d.uniforms[(size_t)sw * n * L + pos]
-                                          : philox_uniform(d.seed, (uint64_t)d.chain_id, sweep_id, (uint64_t)pos);
             }
         }
+        // the next site's row and column are in flight while this one is decided (each thread
+        // copies and later reads only its own rows j)
+        if (i + 1 < n) {
+#pragma unroll
+            for (int q = 0; q < kPer; ++q) {
+                const int j = threadIdx.x + q * kNT;
+                if (j < n) {
+                    async_copy_elem(cnext + j, g + (size_t)j * n + i + 1);
+                    async_copy_elem(rnext + j, g + (size_t)(i + 1) * n + j);
+                }
+            }
+        }
+        async_copy_commit();
         const long long tb = clock64();
         cluster.sync();
         if (threadIdx.x == 0) sm.sub[7] += clock64() - tb;
         const double ratio = sm.gii[par] * sm.gii[par + 1];   // R_up R_dn, the same product in both CTAs
-        const bool acc = (sm.gii[6 + (i & 1)] <= ratio);
+        const bool acc = (uni[i] <= ratio);
         if (sp == 0 && d.record && threadIdx.x == 0) d.decisions[((size_t)sw * L + step) * n + i] = acc ? 1 : 0;
-        if (!acc) continue;
-        const T a = (T)sm.gii[4 + (i & 1)];
+        bool flushed = false;
+        if (acc) {
+            const T a = (T)sm.gii[4 + (i & 1)];
 #pragma unroll
-        for (int q = 0; q < kPer; ++q) {
-            const int j = threadIdx.x + q * kNT;
-            if (j >= n) break;
-            T cu = colv[q], rv = rowv[q];
-            for (int p = 0; p < m; ++p) {
-                cu = fma(-sm.dx[(size_t)j * ld + p], sm.dy[(size_t)i * ld + p], cu);   // G_eff[j][i]
-                rv = fma(-sm.dx[(size_t)i * ld + p], sm.dy[(size_t)j * ld + p], rv);   // G_eff[i][j]
+            for (int q = 0; q < kPer; ++q) {
+                const int j = threadIdx.x + q * kNT;
+                if (j >= n) break;
+                T cu = colv[q], rv = rowv[q];
+                for (int p = 0; p < m; ++p) {
+                    cu = fma(-sm.dx[(size_t)j * ld + p], sm.dy[(size_t)i * ld + p], cu);   // G_eff[j][i]
+                    rv = fma(-sm.dx[(size_t)i * ld + p], sm.dy[(size_t)j * ld + p], rv);   // G_eff[i][j]
+                }
+                sm.dx[(size_t)j * ld + m] = cu;
+                sm.dy[(size_t)j * ld + m] = ((j == i ? T(1) : T(0)) - rv) * a;
             }
-            sm.dx[(size_t)j * ld + m] = cu;
-            sm.dy[(size_t)j * ld + m] = ((j == i ? T(1) : T(0)) - rv) * a;
+            if (threadIdx.x == 0) {
+                f[i] = (int8_t)(-s_il);   // both CTAs write the same value
+                if (sp == 0) ++*accepted;
+            }
+            __syncthreads();
+            if (++m == kd) {
+                // the copies of the next row and column read G before this flush changes it
+                async_copy_wait_all();
+                const long long tf = clock64();
+                GemmOpt<T> o;
+                o.subtract = true;
+                gemm_t<T, EMU, LQMC_FP64E_NATIVE_UPDATE, false, true>(sm, g, n, sm.dx, ld, sm.dy, ld, n, n, m, o);
+                if (threadIdx.x == 0) sm.sub[6] += clock64() - tf;
+                m = 0;
+                flushed = true;
+                for (int j = threadIdx.x; j < n; j += kNT) gdiag[j] = (double)g[(size_t)j * n + j];
+                __syncthreads();
+            }
         }
-        if (threadIdx.x == 0) {
-            f[i] = (int8_t)(-s_il);   // both CTAs write the same value
-            if (sp == 0) ++*accepted;
-        }
-        __syncthreads();
-        if (++m == kd) {
-            const long long tf = clock64();
-            GemmOpt<T> o;
-            o.subtract = true;
-            gemm_t<T, EMU, LQMC_FP64E_NATIVE_UPDATE, false, true>(sm, g, n, sm.dx, ld, sm.dy, ld, n, n, m, o);
-            if (threadIdx.x == 0) sm.sub[6] += clock64() - tf;
-            m = 0;
+        async_copy_wait_all();
+        if (i + 1 < n) {
+#pragma unroll
+            for (int q = 0; q < kPer; ++q) {
+                const int j = threadIdx.x + q * kNT;
+                if (flushed) {   // G changed: the next row and column are read again
+                    colv[q] = (j < n) ? g[(size_t)j * n + i + 1] : T(0);
+                    rowv[q] = (j < n) ? g[(size_t)(i + 1) * n + j] : T(0);
+                } else {
+                    colv[q] = (j < n) ? cnext[j] : T(0);
+                    rowv[q] = (j < n) ? rnext[j] : T(0);
+                }
+            }
         }
     }
     if (m > 0) {
@@ -948,7 +1067,7 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     const int n = d.n;
     const size_t nn = (size_t)n * n;
     const bool xy_global = (d.flags & kUpdatesInGlobal) != 0;
-    TiledLayout<T> lay(n, d.n_chunks, EMU, xy_global ? d.delay : 0);
+    TiledLayout<T> lay(n, d.n_chunks, EMU, xy_global ? d.delay : 0, d.order == LQMC_ORDER_ALTERNATE);
     unsigned char* w = reinterpret_cast<unsigned char*>(d.work);
     unsigned char* wb = w + (size_t)sp * lay.spin_block;   // this spin's block
     TSmem<T> sm;
@@ -989,10 +1108,10 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     sm.oz.stages = d.oz_stages;
     sm.native = d.native;
     if constexpr (EMU) {
-        const size_t pre_off[4] = {lay.pre, lay.pre + lay.pre_a, lay.pre + 2 * lay.pre_a, lay.pre + 3 * lay.pre_a};
-        for (int i = 0; i < 4; ++i) {
-            sm.pre[i].slices = reinterpret_cast<const __nv_bfloat16*>(w + pre_off[i]);
-            sm.pre[i].exps = reinterpret_cast<const int*>(w + lay.pre_e) + i * n;
+        const PresplitLayout pl(n);
+        for (int i = 0; i < kNumPre; ++i) {
+            sm.pre[i].slices = reinterpret_cast<const __nv_bfloat16*>(d.presplit + pl.slices(i));
+            sm.pre[i].exps = reinterpret_cast<const int*>(d.presplit + pl.e) + i * n;
         }
     }
     sm.oz.tc = &tcs;
@@ -1025,23 +1144,7 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
     // the partner CTA's exchange buffers
     sm.peer_gii = cluster.map_shared_rank(sm.gii, (unsigned)(sp ^ 1));
     sm.peer_xv = cluster.map_shared_rank(sm.xv[0], (unsigned)(sp ^ 1));
-    if constexpr (EMU) {
-        // split the constant operands once per launch: CTA 0 e^{-dtau K} as A (straight and
-        // transposed), CTA 1 e^{+dtau K} as A and e^{-dtau K} as B; the cluster barrier below
-        // publishes them to the other CTA
-        int* scratch = reinterpret_cast<int*>(sm.oz.stage);
-        auto pre_slices = [&](int i) { return const_cast<__nv_bfloat16*>(sm.pre[i].slices); };
-        auto pre_exps = [&](int i) { return const_cast<int*>(sm.pre[i].exps); };
-        if (sp == 0) {
-            ozt::presplit(d.expk, n, true, false, n, n, pre_slices(kPreK), pre_exps(kPreK), scratch);
-            ozt::presplit(d.expk, n, true, true, n, n, pre_slices(kPreKT), pre_exps(kPreKT), scratch);
-        } else {
-            ozt::presplit(d.expkinv, n, true, false, n, n, pre_slices(kPreKinv), pre_exps(kPreKinv), scratch);
-            ozt::presplit(d.expk, n, false, false, n, n, pre_slices(kPreKB), pre_exps(kPreKB), scratch);
-        }
-    }
     cluster.sync();   // both CTAs set up before any remote write
-    if constexpr (EMU) asm volatile("fence.proxy.async;\n" ::: "memory");   // the partner's splits
 
     double max_resid = 0.0, logdet = 0.0, sgn = 1.0;
     uint64_t sweep_id = (uint64_t)d.diag[7];
@@ -1054,30 +1157,92 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
         ph[k] += t_ - tc;                   \
         tc = t_;                            \
     } while (0)
-    // sw indexes the call's uniforms and decisions: sweep_base + the sweep of this launch
+    // sw indexes the call's uniforms and decisions: sweep_base + the sweep of this launch.
+    // Alternating order (d.order): state 0 = no valid stacks (build the right stack from
+    // scratch and sweep down), 1 = the next sweep goes up, 2 = the next sweep goes down on the
+    // right products the up sweep left.
+    const bool alt = d.order == LQMC_ORDER_ALTERNATE;
+    const int K = d.n_chunks;
+    int state = alt ? (int)d.diag[21] : 0;
+    auto lslot = [&](int c) { return 2 * K + sp * K + c; };   // alternating: left product at boundary c s
     for (int sw = sweep_base; sw < sweep_base + n_sweeps; ++sw, ++sweep_id) {
-        right_stack_t<T, EMU>(d, sm, sp, &logdet, &sgn, &singular);
-        LQMC_PHASE(0);
-        int lp = 0;
-        for (int c = d.n_chunks - 1; c >= 0; --c) {
-            const int lo = c * d.stab_every, hi = min(lo + d.stab_every, d.L);
-            for (int l = hi - 1; l >= lo; --l) {
-                update_slice_t<T, EMU>(d, sm, l, sw, sweep_id, &accepted);
-                LQMC_PHASE(1);
-                if (l > 0) wrap_t<T, EMU>(d, sm, l);
-                LQMC_PHASE(2);
+        if (!(alt && state == 1)) {
+            // ---- down: l = L-1 .. 0 (the reference's order) ----
+            if (!(alt && state == 2)) right_stack_t<T, EMU>(d, sm, sp, &logdet, &sgn, &singular);
+            LQMC_PHASE(0);
+            int lp = 0;
+            for (int c = K - 1; c >= 0; --c) {
+                const int lo = c * d.stab_every, hi = min(lo + d.stab_every, d.L);
+                for (int l = hi - 1; l >= lo; --l) {
+                    update_slice_t<T, EMU>(d, sm, l, d.L - 1 - l, sw, sweep_id, &accepted);
+                    LQMC_PHASE(1);
+                    if (l > 0 || alt) wrap_t<T, EMU>(d, sm, l);
+                    LQMC_PHASE(2);
+                }
+                if (c > 0) {
+                    int ls;
+                    if (alt) {
+                        ls = lslot(c);
+                        left_step_t<T, EMU>(d, sm, sp, c == K - 1 ? -1 : lslot(c + 1), ls, lo, hi);
+                    } else {
+                        const int in = 2 * K + 2 * sp + lp;
+                        lp ^= 1;
+                        ls = 2 * K + 2 * sp + lp;
+                        left_step_t<T, EMU>(d, sm, sp, c == K - 1 ? -1 : in, ls, lo, hi);
+                    }
+                    const int rs = sp * K + c - 1;
+                    const double r = green_udt_t<T, EMU>(
+                        d, sm, slot_U(sm, rs, nn), slot_d(sm, rs, nn), slot_T(sm, rs, nn),
+                        slot_d(sm, rs, nn)[n], slot_U(sm, ls, nn), slot_d(sm, ls, nn),
+                        slot_T(sm, ls, nn), slot_d(sm, ls, nn)[n], sm.g, true, &logdet, &sgn, &singular);
+                    max_resid = fmax(max_resid, r);
+                    LQMC_PHASE(3);
+                } else if (alt) {
+                    // the bottom turn: G wrapped down to tau = 0 and refreshed as
+                    // G(0) = (1 + B_{L-1} ... B_0)^-1 = ((1 + C^T)^-1)^T from the full left product
+                    const int ls = lslot(0);
+                    left_step_t<T, EMU>(d, sm, sp, K == 1 ? -1 : lslot(1), ls, lo, hi);
+                    transpose_green<T>(sm, n);
+                    const double r = green_udt_t<T, EMU>(
+                        d, sm, slot_U(sm, ls, nn), slot_d(sm, ls, nn), slot_T(sm, ls, nn),
+                        slot_d(sm, ls, nn)[n], nullptr, nullptr, nullptr, 1.0, sm.g, true, &logdet, &sgn,
+                        &singular);
+                    transpose_green<T>(sm, n);
+                    max_resid = fmax(max_resid, r);
+                    LQMC_PHASE(3);
+                }
             }
-            if (c > 0) {
-                left_step_t<T, EMU>(d, sm, sp, lp, c == d.n_chunks - 1, lo, hi);
-                lp ^= 1;
-                const int rs = sp * d.n_chunks + c - 1, ls = 2 * d.n_chunks + 2 * sp + lp;
-                const double r = green_udt_t<T, EMU>(
-                    d, sm, slot_U(sm, rs, nn), slot_d(sm, rs, nn), slot_T(sm, rs, nn),
-                    slot_d(sm, rs, nn)[n], slot_U(sm, ls, nn), slot_d(sm, ls, nn),
-                    slot_T(sm, ls, nn), slot_d(sm, ls, nn)[n], sm.g, true, &logdet, &sgn, &singular);
+            if (alt) state = 1;
+        } else {
+            // ---- up: l = 0 .. L-1; each slice is wrapped into before its sites are visited,
+            // and each chunk's right product becomes the next down sweep's right stack ----
+            for (int c = 0; c < K; ++c) {
+                const int lo = c * d.stab_every, hi = min(lo + d.stab_every, d.L);
+                for (int l = lo; l < hi; ++l) {
+                    wrap_t<T, EMU>(d, sm, l, true);
+                    LQMC_PHASE(2);
+                    update_slice_t<T, EMU>(d, sm, l, l, sw, sweep_id, &accepted);
+                    LQMC_PHASE(1);
+                }
+                const int rs = sp * K + c;
+                right_chunk_t<T, EMU>(d, sm, sp, c, c ? rs - 1 : -1, rs);
+                double r;
+                if (c < K - 1) {
+                    const int ls = lslot(c + 1);
+                    r = green_udt_t<T, EMU>(d, sm, slot_U(sm, rs, nn), slot_d(sm, rs, nn), slot_T(sm, rs, nn),
+                                            slot_d(sm, rs, nn)[n], slot_U(sm, ls, nn), slot_d(sm, ls, nn),
+                                            slot_T(sm, ls, nn), slot_d(sm, ls, nn)[n], sm.g, true, &logdet,
+                                            &sgn, &singular);
+                } else {
+                    // the top turn: G(beta) = (1 + B_{L-1} ... B_0)^-1 from the full right product
+                    r = green_udt_t<T, EMU>(d, sm, slot_U(sm, rs, nn), slot_d(sm, rs, nn), slot_T(sm, rs, nn),
+                                            slot_d(sm, rs, nn)[n], nullptr, nullptr, nullptr, 1.0, sm.g, true,
+                                            &logdet, &sgn, &singular);
+                }
                 max_resid = fmax(max_resid, r);
                 LQMC_PHASE(3);
             }
+            state = 2;
         }
         __syncthreads();
         if (do_measure) measure_t<T>(d, sm);
@@ -1103,6 +1268,7 @@ sweep_tiled_kernel(const ChainDesc* __restrict__ descs, int n_sweeps, int do_mea
             d.diag[1] += (double)n_sweeps * n * d.L;
             d.diag[2] = max_resid;
             d.diag[7] += (double)n_sweeps;
+            if (alt) d.diag[21] = (double)state;
             for (int k = 0; k < 5; ++k) d.diag[8 + k] = (double)ph[k];
             for (int k = 0; k < 8; ++k) d.diag[13 + k] = (double)sub[k];
             if (max_resid > d.drift_tol) atomicOr(d.status, LQMC_STATUS_DRIFT);
@@ -1126,6 +1292,29 @@ static cudaError_t launch_tiled(const ChainDesc* d_descs, int n_chains, size_t s
     sweep_tiled_kernel<T, EMU><<<2 * n_chains, kNT, smem, stream>>>(d_descs, n_sweeps, measure,
                                                                   sweep_base);
     return cudaGetLastError();
+}
+
+// The constant operands of every distinct e^{-dtau K} (PresplitLayout): block kNumPre g + i
+// splits operand i of job g.  Runs once per handle, before the first sweep.
+struct PresplitJob {
+    const double* expk;
+    const double* expkinv;
+    unsigned char* out;
+    int n;
+};
+
+static __global__ void __launch_bounds__(kNT) presplit_kernel(const PresplitJob* jobs) {
+    __shared__ int scratch[ozt::kScratchStripes + 8 * kNT];
+    const PresplitJob j = jobs[blockIdx.x / kNumPre];
+    const int i = blockIdx.x % kNumPre, n = j.n;
+    const PresplitLayout pl(n);
+    __nv_bfloat16* slices = reinterpret_cast<__nv_bfloat16*>(j.out + pl.slices(i));
+    int* exps = reinterpret_cast<int*>(j.out + pl.e) + i * n;
+    if (i == kPreK) ozt::presplit(j.expk, n, true, false, n, n, slices, exps, scratch);
+    else if (i == kPreKT) ozt::presplit(j.expk, n, true, true, n, n, slices, exps, scratch);
+    else if (i == kPreKinv) ozt::presplit(j.expkinv, n, true, false, n, n, slices, exps, scratch);
+    else if (i == kPreKB) ozt::presplit(j.expk, n, false, false, n, n, slices, exps, scratch);
+    else ozt::presplit(j.expkinv, n, false, false, n, n, slices, exps, scratch);
 }
 
 }  // namespace lqmc

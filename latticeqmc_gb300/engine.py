@@ -89,11 +89,19 @@ class Engine:
     measure_tau  also accumulate the unequal-time G(tau_l, 0) of every slice on each measured
                sweep ('dqmc' only; a float64 kernel per sweep after the sweep kernel; read with
                green_tau / green_tau_sum)
+    sweep_order  'down' (every sweep l = L-1 .. 0, the reference's order) or 'alternate'
+               ('dqmc' only, tiled kernel: sweeps alternate down and up, so each direction's
+               UDT products serve the next sweep instead of a from-scratch rebuild; decisions
+               are recorded in visit order; a checkpoint resumes with a rebuild, equal to the
+               uninterrupted run only to rounding)
+    oz_stages  'fp64e': stage buffers of the emulated GEMM's copy / MMA ring (1 .. 3; 0: the
+               engine's rule)
     """
 
     def __init__(self, chains, mode="dqmc", precision="fp64", rng="philox", stab_every=None,
                  delay=0, seed=0, record=False, device=0, engine="auto", debug=0,
-                 fp64e_native=("lu", "lu_rhs"), measure_tau=False):
+                 fp64e_native=("lu", "lu_rhs"), measure_tau=False, sweep_order="down",
+                 oz_stages=0):
         self.chains = list(chains)
         if stab_every is None:
             stab_every = auto_stab_every(self.chains)
@@ -101,8 +109,9 @@ class Engine:
         self.mode, self.precision, self.rng = mode, precision, rng
         self.record = bool(record)
         self.measure_tau = bool(measure_tau)
+        self.sweep_order = sweep_order
         self._h = _native.Handle(mode, precision, rng, stab_every, delay, seed, record, device,
-                                 engine, debug, fp64e_native, measure_tau)
+                                 engine, debug, fp64e_native, measure_tau, sweep_order, oz_stages)
         n = len(self.chains)
         n_sites = np.array([c.n for c in self.chains], dtype=np.int32)
         n_slices = np.array([c.L for c in self.chains], dtype=np.int32)

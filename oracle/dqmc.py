@@ -228,6 +228,118 @@ class Chain:
         return self.green
 
 
+def _slice_rank1(self, g, l, step, uniforms, pos, acc_rec, rat_rec):
+    """Site updates of slice l (visit step `step`) with the rank-1 update of ``sweep``."""
+    for i in range(self.n):
+        s_il = self.field[i, l]
+        dl_up = np.exp(2.0 * self.lamb * s_il) - 1.0
+        dl_dn = np.exp(-2.0 * self.lamb * s_il) - 1.0
+        r_up = 1.0 + dl_up * (1.0 - g[0][i, i])
+        r_dn = 1.0 + dl_dn * (1.0 - g[1][i, i])
+        ratio = r_up * r_dn
+        acc = uniforms[pos] <= ratio
+        pos += 1
+        acc_rec[step, i] = acc
+        rat_rec[step, i] = ratio
+        if acc:
+            for s, dl, r in ((0, dl_up, r_up), (1, dl_dn, r_dn)):
+                gg = g[s]
+                x = gg[:, i].copy()
+                y = -gg[i, :].copy()
+                y[i] += 1.0
+                y *= dl / r
+                g[s] = gg - np.outer(x, y)
+            self.field[i, l] = -s_il
+    return pos
+
+
+def _wrap_up(self, l, g, sigma):
+    """G <- B_l G B_l^-1 = exp_v(l) exp_k G exp_k^-1 exp_v(l)^-1 (from slice l-1 to slice l)."""
+    ev = exp_v_diag(self.field[:, l], self.lamb, sigma)
+    return (ev[:, None] * (self.exp_k @ g @ self.exp_k_inv)) / ev[None, :]
+
+
+def _right_chunk(self, sigma, prev, lo, hi):
+    """UDT of B_{hi-1} ... B_lo R_prev (prev None: identity)."""
+    u, d, t, _ = prev if prev is not None else identity_udt(self.n)
+    z = u
+    for l in range(lo, hi):
+        z = self.b_left(l, sigma, z)
+    return udt_step(z, d, t, self.qr)
+
+
+def sweep_alternating(self, uniforms, record=None):
+    """One sweep of the alternating order: down (l = L-1 .. 0) and up (l = 0 .. L-1) in
+    turn.  A down sweep builds the right stack from scratch only on the first sweep (later
+    the previous up sweep's right products serve), stores the left product at every chunk
+    boundary, wraps below slice 0 and refreshes G(0) = (1 + B_{L-1} ... B_0)^-1 from the full
+    left product; an up sweep wraps into each slice before visiting it
+    (G <- B_l G B_l^-1), absorbs each finished chunk into the right product, refreshes at the
+    chunk boundaries from (right product, stored left product) and at the top from the full
+    right product.  Uniforms and decisions are in visit order."""
+    n, L = self.n, self.L
+    ch = chunks(L, self.stab_every)
+    K = len(ch)
+    state = getattr(self, "alt_state", 0)
+    acc_rec = np.zeros((L, n), np.int8)
+    rat_rec = np.zeros((L, n))
+    self.max_resid = 0.0
+    pos = 0
+    upd = self._update_slice_delayed if self.delay > 0 else self._slice_rank1
+
+    def refresh(s, right, left, g_old):
+        gs, ld, sg = green_from_udt(right, left)
+        self.max_resid = max(self.max_resid, float(np.abs(gs - g_old).max()))
+        self.logdet[s], self.sign[s] = ld, sg
+        return gs
+
+    if state != 1:
+        if state == 0:
+            self.right = [self.right_stack(+1), self.right_stack(-1)]
+            g = []
+            for s in range(2):
+                gs, ld, sg = green_from_udt(self.right[s][-1], identity_udt(n))
+                g.append(gs)
+                self.logdet[s], self.sign[s] = ld, sg
+        else:
+            g = [self.green[0].copy(), self.green[1].copy()]
+        self.left = [[None] * K, [None] * K]
+        for c in reversed(range(K)):
+            lo, hi = ch[c]
+            for l in reversed(range(lo, hi)):
+                pos = upd(g, l, L - 1 - l, uniforms, pos, acc_rec, rat_rec)
+                g = [self.wrap(l, g[0], +1), self.wrap(l, g[1], -1)]
+            for s, sigma in ((0, +1), (1, -1)):
+                prev = self.left[s][c + 1] if c + 1 < K else identity_udt(n)
+                self.left[s][c] = self.left_step(sigma, prev, lo, hi)
+                right = self.right[s][c - 1] if c > 0 else identity_udt(n)
+                g[s] = refresh(s, right, self.left[s][c], g[s])
+        self.alt_state = 1
+    else:
+        g = [self.green[0].copy(), self.green[1].copy()]
+        for c in range(K):
+            lo, hi = ch[c]
+            for l in range(lo, hi):
+                g = [self._wrap_up(l, g[0], +1), self._wrap_up(l, g[1], -1)]
+                pos = upd(g, l, l, uniforms, pos, acc_rec, rat_rec)
+            for s, sigma in ((0, +1), (1, -1)):
+                self.right[s][c] = self._right_chunk(sigma, self.right[s][c - 1] if c else None, lo, hi)
+                left = self.left[s][c + 1] if c + 1 < K else identity_udt(n)
+                g[s] = refresh(s, self.right[s][c], left, g[s])
+        self.alt_state = 2
+    self.green = np.stack(g)
+    if record is not None:
+        record["accept"] = acc_rec
+        record["ratio"] = rat_rec
+    return self.green
+
+
+Chain._slice_rank1 = _slice_rank1
+Chain._wrap_up = _wrap_up
+Chain._right_chunk = _right_chunk
+Chain.sweep_alternating = sweep_alternating
+
+
 def _slice_delayed(self, g, l, step, uniforms, pos, acc_rec, rat_rec):
     """Site updates of slice l with delayed rank-k updates: x = G_eff[:, i],
     y = (Delta/R)(e_i - G_eff[i, :]) with G_eff = G - X Y^T; G -= X Y^T every `delay`

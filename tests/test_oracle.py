@@ -223,3 +223,69 @@ def test_dqmc_ragged_refresh_chunks_agree(L, stabs):
         for (acc, g), (acc0, g0) in zip(out, ref):
             np.testing.assert_array_equal(acc, acc0)
             assert np.abs(g - g0).max() < 1e-11
+
+
+def _square(side):
+    if side in (2, 4):
+        return kinetic_from_golden(side)
+    from latticeqmc_gb300 import HubbardModel
+    m = HubbardModel(u=4, t=1, mu=0)
+    m.build_square(side)
+    return m.ham_kinetic()
+
+
+def test_alternating_sweeps_keep_g_equal_to_a_fresh_recompute():
+    """Sweeps down and up in turn: after every sweep G equals (1 + B_{L-1} .. B_0)^-1 of the
+    field as it now stands, computed from scratch, and the refreshes agree with the wraps."""
+    K = _square(4)
+    beta, L, stab, u = 4.0, 40, 8, 4.0
+    dtau = beta / L
+    lamb = np.arccosh(np.exp(u * dtau / 2.0))
+    ek, eki = expm(-dtau * K), expm(dtau * K)
+    rng = np.random.default_rng(11)
+    field = (2 * rng.integers(0, 2, (16, L)) - 1).astype(np.int8)
+    ch = dqmc.Chain(ek, eki, lamb, field, stab)
+    for sw in range(4):
+        g = ch.sweep_alternating(rng.random(16 * L))
+        ref = dqmc.Chain(ek, eki, lamb, ch.field, stab)
+        for s, sigma in ((0, +1), (1, -1)):
+            gs = dqmc.green_from_udt(ref.right_stack(sigma)[-1], dqmc.identity_udt(16))[0]
+            assert np.abs(g[s] - gs).max() < 1e-12
+        assert ch.max_resid < 1e-9
+        assert ch.alt_state == (1 if sw % 2 == 0 else 2)
+
+
+def test_alternating_up_sweep_ratios_are_determinant_ratios():
+    """Every ratio of an up sweep (2x2, beta=1, L=10: small enough for plain determinants) is
+    det M(flipped) / det M of the configuration the site saw: slices below already updated,
+    its own slice updated up to the site, the rest as before the sweep."""
+    K = _square(2)
+    beta, L, stab, u = 1.0, 10, 4, 4.0
+    dtau = beta / L
+    lamb = np.arccosh(np.exp(u * dtau / 2.0))
+    ek = expm(-dtau * K)
+    rng = np.random.default_rng(5)
+    field = (2 * rng.integers(0, 2, (4, L)) - 1).astype(np.int8)
+    ch = dqmc.Chain(ek, expm(dtau * K), lamb, field, stab)
+    ch.sweep_alternating(rng.random(4 * L))          # down
+    before = ch.field.copy()
+    rec = {}
+    ch.sweep_alternating(rng.random(4 * L), record=rec)   # up
+
+    def det_both(f):
+        tot = 1.0
+        for sigma in (+1, -1):
+            m = np.eye(4)
+            for ll in range(L):
+                m = dqmc.exp_v_diag(f[:, ll], lamb, sigma)[:, None] * (ek @ m)
+            tot *= np.linalg.det(np.eye(4) + m)
+        return tot
+    cfg = before.copy()
+    for l in range(L):
+        for i in range(4):
+            fl = cfg.copy()
+            fl[i, l] *= -1
+            np.testing.assert_allclose(rec["ratio"][l, i], det_both(fl) / det_both(cfg), rtol=1e-10)
+            if rec["accept"][l, i]:
+                cfg = fl
+    np.testing.assert_array_equal(cfg, ch.field)
