@@ -33,7 +33,7 @@ def test_fastest_setting_meeting_the_bar_is_chosen_and_cached(tmp_path, monkeypa
     cache = tmp_path / "t.json"
     rec = at.autotune(16, 8.0, 80, "fp64e", candidates=cands, cache=str(cache), log=None)
     assert rec["chosen"]["stab_every"] == 8 and rec["chosen"]["sweep_order"] == "alternate"
-    assert rec["runner_up"]["stab_every"] == 8 and rec["runner_up"]["sweep_order"] == "down"
+    assert rec["runner_up"]["stab_every"] == 6 and rec["runner_up"]["sweep_order"] == "alternate"
     assert at.tuned(16, 8.0, 80, "fp64e", cache=str(cache))["chosen"] == rec["chosen"]
     assert at.settings(rec) == {"stab_every": 8, "delay": 0, "sweep_order": "alternate", "oz_stages": 0}
     assert json.loads(cache.read_text())["square16_beta8_L80_fp64e"]["shape"] == rec["shape"]
