@@ -337,17 +337,18 @@ def time_engine(torch, specs, precision, stab, steps, warmup, stream, seed, dev,
     return out
 
 
-def green_difference(specs, stab, dev, precision, sweeps=1, seed=77):
+def green_difference(specs, stab, dev, precision, sweeps=1, seed=77, **kw):
     """`precision` against fp64 over `sweeps` sweeps from identical fields and uniforms:
     per sweep max|G_precision - G_fp64| over all chains and over the chains whose decisions
     have all agreed so far (the pure precision effect), the number of such chains, and the
     status bits and stabilisation residuals of both engines at the end."""
     from latticeqmc_gb300 import Engine
     rng = np.random.default_rng(seed)
+    ref_kw = {k: v for k, v in kw.items() if k == "sweep_order"}
     a = Engine(specs, mode="dqmc", precision="fp64", rng="replay", stab_every=stab, device=dev,
-               record=True)
+               record=True, **ref_kw)
     b = Engine(specs, mode="dqmc", precision=precision, rng="replay", stab_every=stab, device=dev,
-               record=True)
+               record=True, **kw)
     total = sum(c.n * c.L for c in specs)
     same = np.ones(len(specs), bool)
     per_sweep, per_sweep_same = [], []
@@ -383,9 +384,10 @@ def green_difference(specs, stab, dev, precision, sweeps=1, seed=77):
     return out
 
 
-def time_e2e(torch, specs, stab, steps, warmup, stream, dev, world, rank, precision):
+def time_e2e(torch, specs, stab, steps, warmup, stream, dev, world, rank, precision, **kw):
     from latticeqmc_gb300 import Engine
-    eng = Engine(specs, mode="dqmc", precision=precision, rng="replay", stab_every=stab, device=dev)
+    eng = Engine(specs, mode="dqmc", precision=precision, rng="replay", stab_every=stab, device=dev,
+                 **kw)
     total_uni = sum(c.n * c.L for c in specs)
     total_g = sum(2 * c.n * c.n for c in specs)
     steps_all = warmup + steps
@@ -476,6 +478,43 @@ def square32(torch, stream, dev, world, rank, steps=1, warmup=1):
             "steps": steps, "warmup": warmup, "gpu_launches": r["launches"]}
 
 
+STAB_RANGE = {"square16_beta8": (8, 16)}   # stabilisation intervals the workload allows
+
+
+def tuned_settings(args, cfg, precision):
+    """Engine settings of the headline engine and the tuning record behind them."""
+    from latticeqmc_gb300 import autotune
+    default = {"stab_every": cfg["stab_every"], "sweep_order": "alternate"}
+    if args.workload == "batched_fp64":
+        return {}, None
+    rec = autotune.tuned(cfg["sides"][0], cfg["beta"], cfg["L"], precision)
+    lo, hi = STAB_RANGE.get(args.workload, (1, 10 ** 6))
+    if rec is None:
+        return default, {"source": "no autotuner record for this shape: defaults"}
+    passing = sorted((r for r in rec["candidates"]
+                      if r.get("ok") and lo <= r["stab_every"] <= hi),
+                     key=lambda r: r["seconds_per_sweep"])
+    if not passing:
+        return default, {"source": "no autotuner candidate in the allowed stabilisation range "
+                                   "met the accuracy constraint: defaults",
+                         "record_chosen": rec["chosen"]}
+    kw = {"stab_every": passing[0]["stab_every"], "sweep_order": passing[0]["sweep_order"]}
+    if passing[0].get("delay"):
+        kw["delay"] = passing[0]["delay"]
+    if passing[0].get("oz_stages"):
+        kw["oz_stages"] = passing[0]["oz_stages"]
+    keep = ("stab_every", "delay", "oz_stages", "sweep_order", "seconds_per_sweep", "max_dG",
+            "chains_flagged")
+    return kw, {"source": "latticeqmc_gb300/tuning/autotune.json (project autotuner, "
+                          f"{rec['chains']} chains, constraint max|dG| <= {rec['tol']} against fp64 "
+                          "and no status flag; stab_every restricted to the workload's range "
+                          f"{lo}-{hi})",
+                "chosen": {k: passing[0].get(k) for k in keep},
+                "runner_up": ({k: passing[1].get(k) for k in keep} if len(passing) > 1 else None),
+                "candidates_tried": len(rec["candidates"]),
+                "candidates_passing": sum(1 for r in rec["candidates"] if r.get("ok"))}
+
+
 def run_ours(args, rank, world):
     import torch
     dev = int(os.environ.get("LOCAL_RANK", 0))
@@ -492,24 +531,33 @@ def run_ours(args, rank, world):
     stream = torch.cuda.Stream()
     seed = 12345 + 1000003 * rank
     headline = "fp64" if args.workload == "batched_fp64" else "fp64e"
+    # launch settings of the headline engine: the autotuner's choice for this shape when its
+    # cache holds one with stab_every in the workload's allowed range, else the defaults
+    kw, tuning = tuned_settings(args, cfg, headline)
+    stab = kw.pop("stab_every", stab)
+    cfg["stab_every"] = stab
+    cfg["sweep_order"] = kw.get("sweep_order", "down")
     main = time_engine(torch, specs, headline, stab, args.steps, args.warmup, stream, seed, dev,
-                       world, sample_clocks=True)
+                       world, sample_clocks=True, **kw)
+    order_kw = {"sweep_order": kw["sweep_order"]} if "sweep_order" in kw else {}
     others, subs = {}, {}
     if args.workload == "square16_beta8":
-        acc = green_difference(specs, stab, dev, "fp64e", sweeps=args.accuracy_sweeps)
+        acc = green_difference(specs, stab, dev, "fp64e", sweeps=args.accuracy_sweeps, **kw)
         main["accuracy"] = acc
         for prec, key in (("fp64", "fp64"), ("mixed", "fp32_mixed")):
-            o = time_engine(torch, specs, prec, stab, args.steps, args.warmup, stream, seed, dev, world)
+            # the other engines on the same workload, stabilisation interval and sweep order
+            o = time_engine(torch, specs, prec, stab, args.steps, args.warmup, stream, seed, dev, world,
+                            **order_kw)
             od = dict(ms_per_step=o["ms"], status=o["status"],
                       max_stabilisation_residual=o["resid"])
             if prec != "fp64":
-                od.update(green_difference(specs, stab, dev, prec, sweeps=1))
+                od.update(green_difference(specs, stab, dev, prec, sweeps=1, **order_kw))
             others[key] = od
         if not args.no_subrecords:
             subs["batched_fp64"] = batched_vs_sequential(torch, stream, dev, world, rank)
             subs["square32_beta6"] = square32(torch, stream, dev, world, rank)
     e2e_ms, h2d, d2h = time_e2e(torch, specs, stab, args.steps, args.warmup, stream, dev, world,
-                                rank, headline)
+                                rank, headline, **kw)
     peak = fp64_peak_tflops(torch) if rank == 0 else None
     return dict(ms=main["ms"], sites=sum(c.n * c.L for c in specs), chains=len(specs),
                 flops=algorithmic_flops(specs, main["accepted"], stab), launches=main["launches"],
@@ -517,7 +565,7 @@ def run_ours(args, rank, world):
                 resid=main["resid"], resid_median=main["resid_median"], status=main["status"],
                 peak=peak, specs=specs, phases=main["phases"], subs_cycles=main["subs"],
                 others=others, subrecords=subs, headline=headline,
-                accuracy=main.get("accuracy"))
+                accuracy=main.get("accuracy"), tuning=tuning)
 
 
 def roofline(r, args):
@@ -580,6 +628,7 @@ def make_line(args, r, world, cpu):
                        median_stabilisation_residual=r["resid_median"]),
         "phase_share": {k: v / tot for k, v in r["phases"].items()},
         "sub_share": {k: v / tot for k, v in r["subs_cycles"].items()},
+        "tuning": r.get("tuning"),
     }
     if r.get("accuracy"):
         acc = dict(r["accuracy"])
