@@ -310,6 +310,28 @@ typedef struct lqmc_static_chain {
 /* Run n_sweeps dqmc sweeps of the chain described by *chain without allocating memory. */
 int lqmc_sweep_static(const lqmc_static_chain* chain, int32_t n_sweeps, void* stream);
 
+/* ---- the emulated float64 GEMM on its own --------------------------------------------------
+ * No counterpart in the reference (its products are numpy's np.dot, lqmc/lqmc.py:182, :342-345):
+ * one product through the emulated float64 GEMM of the fp64e sweep kernel -- eight BF16 digit
+ * slices per operand on the tcgen05 tensor cores, the same single-CTA pipeline and staging as a
+ * chain's CTA in the sweep -- so that it can be checked against float64 and timed on its own.
+ * Host arrays, row-major: C (m x n, ldc) = op(A) op(B), A(i, p) = trans_a ? a[p lda + i] :
+ * a[i lda + p], B(p, j) = trans_b ? b[j ldb + p] : b[p ldb + j]; with LQMC_GEMM_SUBTRACT,
+ * C -= the product instead; row_scale / col_scale (optional, m / n values) scale the product's
+ * rows / columns first.  stages: 1 .. 3 stage buffers.  cycles (optional, 3 values): SM clock
+ * cycles of operand splitting, of the whole product pipeline, and of the accumulator drain
+ * (one epilogue warp).  Returns LQMC_OK, LQMC_ERR_INVALID, LQMC_ERR_CUDA, LQMC_ERR_NOMEM, or
+ * LQMC_ERR_NUMERIC when a bounded wait of the pipeline ran out (C is then not valid).
+ * Allocates and synchronises: a check and measurement tool, not a hot-path call. */
+#define LQMC_GEMM_SUBTRACT 1     /* C -= op(A) op(B)                                            */
+#define LQMC_GEMM_KSCALE 2       /* equilibrate along k (the LU's trailing updates use this)    */
+#define LQMC_GEMM_PRESPLIT_A 4   /* split A in a separate pass first (as the constant operands) */
+#define LQMC_GEMM_PRESPLIT_B 8
+int lqmc_emulated_gemm(int32_t m, int32_t n, int32_t k, const double* a, int32_t lda,
+                       int32_t trans_a, const double* b, int32_t ldb, int32_t trans_b,
+                       double* c, int32_t ldc, const double* row_scale, const double* col_scale,
+                       int32_t flags, int32_t stages, int32_t device, double* cycles);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,6 +22,7 @@ ENGINES = {"auto": 0, "smem": 1, "tiled": 2}
 ORDERS = {"down": 0, "alternate": 1}
 STATUS_NONFINITE, STATUS_SINGULAR, STATUS_DRIFT, STATUS_TIMEOUT = 1, 2, 4, 8
 DEBUG_STALL_TC_WAIT = 1
+GEMM_SUBTRACT, GEMM_KSCALE, GEMM_PRESPLIT_A, GEMM_PRESPLIT_B = 1, 2, 4, 8
 FP64E_NATIVE = {"wrap": 1, "stack": 2, "udt": 4, "green": 8, "update": 16, "lu": 32,
                 "lu_rhs": 64}
 OBS_HEADER = 8
@@ -76,6 +77,8 @@ _SIGS = [
     ("lqmc_last_error", ctypes.c_char_p, [_P]),
     ("lqmc_destroy", None, [_P]),
     ("lqmc_sweep_static", ctypes.c_int, [_P, _I32, _P]),
+    ("lqmc_emulated_gemm", ctypes.c_int, [_I32, _I32, _I32, _P, _I32, _I32, _P, _I32, _I32, _P,
+                                          _I32, _P, _P, _I32, _I32, _I32, _P]),
 ]
 EXPORTED = [s[0] for s in _SIGS]
 
@@ -163,3 +166,32 @@ class Handle:
 
 def as_f64(a):
     return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def emulated_gemm(a, b, c=None, trans_a=False, trans_b=False, subtract=False, row_scale=None,
+                  col_scale=None, kscale=False, presplit_a=False, presplit_b=False, stages=2,
+                  device=0):
+    """C = op(A) op(B) (or C - op(A) op(B)) through the fp64e engine's emulated float64 GEMM
+    on the tensor cores (lqmc_emulated_gemm).  a, b: 2-D float64 arrays as stored (op = the
+    transpose when trans_*).  Returns (C, cycles of split / pipeline / drain)."""
+    lib = load()
+    a = as_f64(a)
+    b = as_f64(b)
+    m = a.shape[1] if trans_a else a.shape[0]
+    k = a.shape[0] if trans_a else a.shape[1]
+    n = b.shape[0] if trans_b else b.shape[1]
+    if (b.shape[1] if trans_b else b.shape[0]) != k:
+        raise ValueError("inner dimensions differ")
+    c = np.zeros((m, n)) if c is None else as_f64(c).copy()
+    rs = None if row_scale is None else as_f64(row_scale)
+    cs = None if col_scale is None else as_f64(col_scale)
+    cyc = np.zeros(3)
+    flags = ((GEMM_SUBTRACT if subtract else 0) | (GEMM_KSCALE if kscale else 0) |
+             (GEMM_PRESPLIT_A if presplit_a else 0) | (GEMM_PRESPLIT_B if presplit_b else 0))
+    rc = lib.lqmc_emulated_gemm(m, n, k, ptr(a), a.shape[1], int(trans_a), ptr(b), b.shape[1],
+                                int(trans_b), ptr(c), n, None if rs is None else ptr(rs),
+                                None if cs is None else ptr(cs), flags, int(stages), int(device),
+                                ptr(cyc))
+    if rc != LQMC_OK:
+        raise LqmcError(rc, "lqmc_emulated_gemm failed")
+    return c, cyc

@@ -38,7 +38,7 @@ namespace {
 
 constexpr int kMaxSitesSmem = 128;    // one-CTA shared-memory kernel (both modes)
 constexpr int kMaxSitesTiled = 1024;  // tiled kernel (dqmc mode): 4 rows per thread
-constexpr int kMaxOzStages = 2;       // stage buffers of the emulated GEMM
+constexpr int kMaxOzStages = 3;       // stage buffers of the emulated GEMM
 
 // which sweep kernel runs a chain
 enum Kind : int { kSmemFp64 = 0, kTiledFp64 = 1, kTiledFp32 = 2, kTiledFp64e = 3 };

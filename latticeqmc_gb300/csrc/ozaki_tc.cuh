@@ -10,23 +10,28 @@
 // maximum, finer than float64's own rounding, and the rounding and the dropped pairs
 // (t + u >= 8, below 2^-60) have either sign, so their errors do not accumulate
 // systematically over k.  Each A_t B_u is a tcgen05.mma (kind::f16, BF16 x BF16 -> FP32,
-// M = 128, K = 16) accumulating into the TMEM columns of diagonal d, so the eight
-// accumulators of a 128 x 64 output tile fill the 512 TMEM columns.  The FP32 sums are exact
+// M = 128, K = 16) accumulating into the TMEM columns of diagonal d: the eight accumulators
+// of a 128 x 32 output tile take 256 TMEM columns, two tiles the SM's 512.  The FP32 sums are exact
 // integers while |D_d| <= 8 k 64^2 <= 2^24, i.e. for k <= kMaxK = 512; longer products are cut
 // into chunks of kMaxK whose results are added in float64.  A row (column) holding a NaN or
 // Inf gives NaN in its output row (column).
 //
 // Data movement: the split writes every slice directly in the tensor core's canonical
 // K-major, no-swizzle layout (8 x 16-byte core matrices), grouped so that all eight slices
-// of one (row block, 16-wide k step) are one contiguous block.  One thread then moves a
-// whole k step of A (32 KB) and of B (16 KB) into shared memory with two bulk asynchronous
-// copies completing on an mbarrier, issues the step's MMAs (one per A digit t, N = 64 (8 - t)
-// cut at 256: 12 instructions for the 36 digit pairs) and commits them to a second mbarrier;
-// with two stage buffers the copies of step s + 1 overlap the MMAs of step s.  The epilogue
-// reads the accumulators with tcgen05.ld (warp w reads TMEM lanes 32 (w mod 4) ..), combines
-// them in int64 and converts to float64 with integer operations, the scale folded into the
-// exponent.
-//
+// of one (row block, 16-wide k step) are one contiguous block; B's slices of a 32-column block
+// stack into one 256-row operand.  The product then runs as a warp-specialised pipeline over
+// 128 x 32 output tiles (x k chunks of kMaxK):
+//   warp 1 (one thread)   streams each k step of A (32 KB) and B (8 KB) into a ring of
+//                         `stages` shared-memory stage buffers, two bulk asynchronous copies
+//                         per stage completing on the stage's `full` mbarrier;
+//   warp 0 (one thread)   issues the step's MMAs -- one per A digit t, A_t times the stacked
+//                         B_0 .. B_{7-t} (N = 32 (8 - t)) -- into one of two TMEM accumulator
+//                         buffers (the 8 diagonals of a tile take 256 columns), commits each
+//                         step to the stage's `empty` mbarrier and each tile to `acc_full`;
+//   warps 4..7            drain a finished buffer (warp w reads TMEM lanes 32 (w mod 4) ..)
+//                         while the MMAs of the next tile fill the other, combine the digits
+//                         in int64, convert to float64 with integer operations (the scale
+//                         folded into the exponent) and write C, then release the buffer.
 // Every wait is bounded: a wait that runs out sets Tc::fail, after which this and every later
 // call return without issuing work; the kernel reports the flag as a status bit.
 #pragma once
@@ -45,13 +50,18 @@ using namespace blk;
 constexpr int kSlices = 8;
 constexpr int kBits = 7;
 constexpr int kWidth = kSlices * kBits - 1;   // 55: the top digit absorbs the rounding carry
-constexpr int kBM = 128, kBN = 64, kBK = 16;
+constexpr int kBM = 128, kBN = 32, kBK = 16;
 constexpr int kTileA = kBM * kBK;             // bf16 elements of one slice tile of A (4 KB)
-constexpr int kTileB = kBN * kBK;             // one slice tile of B (2 KB)
+constexpr int kTileB = kBN * kBK;             // one slice tile of B (1 KB)
 constexpr int kStepA = kSlices * kTileA;      // all slices of one (row block, k step)
 constexpr int kStepB = kSlices * kTileB;
 constexpr int kMaxK = 512;                    // exact FP32 diagonal sums up to this k
-constexpr int kTmemCols = kSlices * kBN;      // 512: the whole tensor memory of the SM
+constexpr int kAccCols = kSlices * kBN;       // 256: the eight diagonals of one output tile
+constexpr int kTmemCols = 2 * kAccCols;       // 512: two accumulator buffers, the whole TMEM
+constexpr int kMaxStages = 3;                 // stage buffers of the copy / MMA ring
+constexpr int kEpiWarp0 = 4;                  // warps 4..7 drain the accumulators (TMEM lane
+                                              // quadrant = warp % 4); warp 0 issues the MMAs,
+                                              // warp 1 the copies
 constexpr int kNonFinite = 1 << 20;
 
 // The epilogue drops the 12 low bits of the combined diagonals (so that the sum fits int64).
@@ -65,7 +75,7 @@ constexpr int kNonFinite = 1 << 20;
 constexpr long long kLowRound = LQMC_OZ_ROUND_EPILOGUE ? (1ll << 11) : 0;
 constexpr long long kWaitCycles = 2000000000ll;   // ~1 s of SM clock before a wait gives up
 
-// shared-memory bytes of `stages` stage buffers (1 or 2)
+// shared-memory bytes of `stages` stage buffers (1 .. kMaxStages)
 __host__ __device__ constexpr size_t stage_bytes(int stages) {
     return (size_t)stages * (kStepA + kStepB) * sizeof(__nv_bfloat16);
 }
@@ -85,10 +95,18 @@ __device__ __forceinline__ int core_offset(int r, int q) {
 }
 
 // per-CTA state of the tensor-core path (static shared memory of the kernel)
+// The pipeline's barriers complete once per use; a waiter for the u-th completion (u >= 1)
+// waits on parity (u - 1) & 1.  `steps` and `units` count the k steps and accumulation units
+// (output tile x k chunk) of all earlier calls, so every role derives its parities from them.
 struct Tc {
-    unsigned long long bar[4];   // copies done [2], MMAs done [2]
+    unsigned long long full[kMaxStages];    // stage loaded (bulk-copy transaction count)
+    unsigned long long empty[kMaxStages];   // the MMAs that read the stage have completed
+    unsigned long long acc_full[2];         // accumulator buffer complete (MMA commit)
+    unsigned long long acc_empty[2];        // accumulator buffer drained (one arrival per
+                                            // epilogue warp)
     uint32_t tmem;               // TMEM base address (lane 0, first column)
-    uint32_t phase;              // parity bits of the four barriers (thread 0)
+    uint32_t steps;              // k steps of all earlier calls
+    uint32_t units;              // accumulation units of all earlier calls
     int fail;                    // a wait ran out
     int stall;                   // test hook: the next step issues no copies (its wait runs out)
 };
@@ -98,9 +116,10 @@ struct Workspace {
     int* ea;                 // m
     int* eb;                 // n
     unsigned char* stage;    // stage_bytes(stages) of shared memory, 128-byte aligned
-    int stages;              // 1 or 2
+    int stages;              // 1 .. kMaxStages
     Tc* tc;
-    long long* cycles;       // optional [3]: splitting, whole product loop, its epilogues (thread 0)
+    long long* cycles;       // optional [3]: splitting, whole product pipeline, the epilogue
+                             // warps' combine and write-out (first epilogue warp)
 };
 
 // An operand split once and reused (constant matrices): its slices in the tile layout of
@@ -124,9 +143,17 @@ __device__ inline void tc_setup(Tc* tc) {
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
     if (threadIdx.x == 0) {
-        for (int i = 0; i < 4; ++i)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&tc->bar[i])));
-        tc->phase = 0;
+        for (int i = 0; i < kMaxStages; ++i) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&tc->full[i])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&tc->empty[i])));
+        }
+        for (int b = 0; b < 2; ++b) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" :: "r"(smem_u32(&tc->acc_full[b])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n"
+                         :: "r"(smem_u32(&tc->acc_empty[b])), "r"(kNW - kEpiWarp0));
+        }
+        tc->steps = 0;
+        tc->units = 0;
         tc->fail = 0;
         tc->stall = 0;
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -146,8 +173,10 @@ __device__ inline void tc_teardown(Tc* tc) {
                      :: "r"(tc->tmem), "r"(kTmemCols));
 }
 
-// bounded parity wait; false when about kWaitCycles passed without the phase completing
-__device__ __forceinline__ bool bar_wait(unsigned long long* bar, uint32_t parity) {
+// bounded parity wait; false when about kWaitCycles passed without the phase completing, or
+// when another role of the pipeline has already given up (fail != 0)
+__device__ __forceinline__ bool bar_wait(unsigned long long* bar, uint32_t parity,
+                                         const volatile int* fail = nullptr) {
     const uint32_t a = smem_u32(bar);
     const long long t0 = clock64();
     for (;;) {
@@ -158,8 +187,12 @@ __device__ __forceinline__ bool bar_wait(unsigned long long* bar, uint32_t parit
             "selp.u32 %0, 1, 0, p;\n\t}\n"
             : "=r"(done) : "r"(a), "r"(parity) : "memory");
         if (done) return true;
-        if (clock64() - t0 > kWaitCycles) return false;
+        if ((fail && *fail) || clock64() - t0 > kWaitCycles) return false;
     }
+}
+
+__device__ __forceinline__ void bar_arrive(unsigned long long* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" :: "r"(smem_u32(bar)) : "memory");
 }
 
 // ---- splitting ---------------------------------------------------------------------------
@@ -480,169 +513,219 @@ __device__ __forceinline__ void oz_gemm_tc_impl(double* c, int ldc, const double
         ksb = cb;
     }
     if (!pa) split_tiles<kBM>(a, lda, TA, m, k, ws.ea, ws.slices, scratch, ksa);
-    if (!pb) split_tiles<kBN>(b, ldb, !TB, n, k, ws.eb, ws.slices + (size_t)kSlices * rows_pad(m, kBM) * kp, scratch, ksb);
-    // the slices were written through the generic proxy and are read by bulk copies
+    if (!pb) split_tiles<kBN>(b, ldb, !TB, n, k, ws.eb, ws.slices + (size_t)kSlices * rows_pad(m, kBM) * kp,
+                              scratch, ksb);
+    // the slices were written through the generic proxy and are read by bulk copies; the
+    // stage served as scratch and is next written by bulk copies
     asm volatile("fence.proxy.async;\n" ::: "memory");
     __syncthreads();
     const long long t1 = clock64();
     if (ws.cycles && threadIdx.x == 0) ws.cycles[0] += t1 - t0;
 
+    // ---- the pipeline: units = (output tile, k chunk of kMaxK), tiles column-major -------
     const int stages = ws.stages;
     const uint32_t tmem = tc->tmem;
     const int tiles_m = rows_pad(m, kBM) / kBM, tiles_n = rows_pad(n, kBN) / kBN;
-    const int chunk_steps = kMaxK / kBK;
+    const int chunk_steps = kMaxK / kBK, n_chunks = (S + chunk_steps - 1) / chunk_steps;
+    const int n_units = tiles_m * tiles_n * n_chunks;
+    const uint32_t step0 = tc->steps, unit0 = tc->units;
     const int w = warp_id(), lane = lane_id();
-    const int row = 32 * (w & 3) + lane;          // TMEM lane = output row of the tile
-    bool failed = false;
-    for (int tile = 0; tile < tiles_m * tiles_n; ++tile) {
-        const int tm = tile / tiles_n, tn = tile % tiles_n;
-        const int i0 = tm * kBM, j0 = tn * kBN;
-        for (int s0 = 0; s0 < S; s0 += chunk_steps) {
-            const int steps = min(chunk_steps, S - s0);
-            if (threadIdx.x == 0 && !failed) {
-                uint32_t ph = tc->phase;
-                auto load = [&](int s, int buf) {
-                    unsigned char* st = stage + (size_t)buf * (kStepA + kStepB) * 2;
-                    expect_tx(&tc->bar[buf], (kStepA + kStepB) * 2);
-                    bulk_load(st, sa + (size_t)(tm * S + s0 + s) * kStepA, kStepA * 2, &tc->bar[buf]);
-                    bulk_load(st + kStepA * 2, sb + (size_t)(tn * S + s0 + s) * kStepB, kStepB * 2, &tc->bar[buf]);
-                };
-                auto wait = [&](int i) -> bool {
-                    const bool ok = bar_wait(&tc->bar[i], (ph >> i) & 1u);
-                    ph ^= 1u << i;
-                    return ok;
-                };
-                if (tc->stall) tc->stall = 0;   // test hook: nothing will complete the first wait
-                else for (int s = 0; s < min(stages, steps); ++s) load(s, s);
-                for (int s = 0; s < steps && !failed; ++s) {
-                    const int buf = s % stages;
-                    if (!wait(buf)) { failed = true; break; }
-                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                    const uint32_t st = smem_u32(stage + (size_t)buf * (kStepA + kStepB) * 2);
-                    // A_t times the stacked B_0 .. B_{7-t}: the accumulators of diagonals
-                    // t .. 7 are the contiguous TMEM columns [64 t, 512), so one MMA of
-                    // N = 64 (8 - t) (cut at 256) covers every pair of this t
-#pragma unroll
-                    for (int t = 0; t < kSlices; ++t) {
-                        constexpr int kMaxN = 256;
-#pragma unroll
-                        for (int off = 0; off < (kSlices - t) * kBN; off += kMaxN) {
-                            const int nn = min(kMaxN, (kSlices - t) * kBN - off);
-                            mma(tmem + (uint32_t)(t * kBN + off), smem_desc(st + t * kTileA * 2),
-                                smem_desc(st + kStepA * 2 + (off / kBN) * kTileB * 2), idesc(nn),
-                                (s > 0 || t > 0) ? 1u : 0u);
-                        }
-                    }
-                    commit(&tc->bar[2 + buf]);
-                    if (stages == 2) {
-                        if (s >= 1) {
-                            if (!wait(2 + (s - 1) % 2)) { failed = true; break; }
-                            if (s + 1 < steps) load(s + 1, (s + 1) % 2);
-                        }
-                    } else {
-                        if (!wait(2)) { failed = true; break; }
-                        if (s + 1 < steps) load(s + 1, 0);
-                    }
-                }
-                if (!failed && stages == 2 && !wait(2 + (steps - 1) % 2)) failed = true;
-                tc->phase = ph;
-                if (failed) tc->fail = 1;
+    volatile int* fail = &tc->fail;
+    // unit u: tile (tm, tn), chunk steps [c0, c0 + cs)
+    auto unit_of = [&](int u, int& tm, int& tn, int& c0, int& cs) {
+        const int tile = u / n_chunks, ch = u % n_chunks;
+        tm = tile % tiles_m;
+        tn = tile / tiles_m;
+        c0 = ch * chunk_steps;
+        cs = min(chunk_steps, S - c0);
+    };
+    constexpr uint32_t kStageBytes = (kStepA + kStepB) * 2;
+    if (w == 1 && lane == 0) {
+        // producer: one k step of A (all slices of a 128-row block) and of B (of a 32-column
+        // block) per stage, two bulk copies completing on the stage's `full` barrier
+        uint32_t g = step0;
+        bool stall = tc->stall != 0;
+        tc->stall = 0;
+        for (int u = 0; u < n_units && !*fail; ++u) {
+            int tm, tn, c0, cs;
+            unit_of(u, tm, tn, c0, cs);
+            for (int s = 0; s < cs; ++s, ++g) {
+                const int i = g % stages;
+                const uint32_t use = g / stages;
+                if (use >= 1 && !bar_wait(&tc->empty[i], (use - 1) & 1, fail)) { *fail = 1; break; }
+                if (stall) { stall = false; continue; }   // test hook: this stage never fills
+                unsigned char* st = stage + (size_t)i * kStageBytes;
+                expect_tx(&tc->full[i], kStageBytes);
+                bulk_load(st, sa + (size_t)(tm * S + c0 + s) * kStepA, kStepA * 2, &tc->full[i]);
+                bulk_load(st + kStepA * 2, sb + (size_t)(tn * S + c0 + s) * kStepB, kStepB * 2, &tc->full[i]);
             }
-            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-            __syncthreads();
-            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            if (tc->fail) return;
-            const long long te = clock64();
-            // epilogue, in two halves of 32 columns: each thread combines 16 outputs of its
-            // row (two groups of 8 columns, all 8 diagonals read before one wait), the half is
-            // transposed through the stage buffer, and written with whole-row coalesced stores
-            double* ts = reinterpret_cast<double*>(stage);   // [kBM][kTs]
-            constexpr int kTs = 33;
-            const int ei = (i0 + row < m) ? ea[i0 + row] : 0;
-            // |D_d| <= 8 k 64^2 < 2^22 for the k of this chunk
-            const bool magic_ok = steps * kBK * 8 * 64 * 64 < (1 << 22);
-#pragma unroll 1
-            for (int h = 0; h < 2; ++h) {
-                if (j0 + 32 * h >= n) break;   // the whole half lies outside C (uniform)
-#pragma unroll 1
-                for (int g = 0; g < 2; ++g) {
-                    const int cl = 16 * (w >> 2) + 8 * g;   // column within the half
-                    const int ct = 32 * h + cl;             // column within the tile
-                    // a warp whose 32 rows or 8 columns all lie outside C skips them (the
-                    // condition is uniform over the warp, as the collective TMEM load needs)
-                    if (j0 + ct >= n || i0 + 32 * (w & 3) >= m) continue;
-                    int ej[8];
-#pragma unroll
-                    for (int x = 0; x < 8; ++x) ej[x] = (j0 + ct + x < n) ? eb[j0 + ct + x] : 0;
-                    uint32_t r[kSlices][8];
-#pragma unroll
-                    for (int d = 0; d < kSlices; ++d)
-                        tmem_ld8(tmem + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)(d * kBN + ct), r[d]);
-                    tmem_wait();
-#pragma unroll
-                    for (int x = 0; x < 8; ++x) {
-                        // T = sum_d D_d 2^(7 (7 - d)) / 2^12 from two Horner halves (|D_d| <= 2^24,
-                        // each half < 2^46); the 12 dropped low bits are 2^-60 of the largest sum
-                        // the exact FP32 integers to int32: below 2^22 (k <= 127) by the 1.5 2^23
-                        // magic number on the FMA / ALU pipes, else by F2I on the XU pipe
-                        int q[kSlices];
-                        if (magic_ok) {
-#pragma unroll
-                            for (int d = 0; d < kSlices; ++d)
-                                q[d] = __float_as_int(__uint_as_float(r[d][x]) + 12582912.0f) - 0x4B400000;
-                        } else {
-#pragma unroll
-                            for (int d = 0; d < kSlices; ++d) q[d] = __float2int_rn(__uint_as_float(r[d][x]));
-                        }
-                        long long hi = q[0], lo = q[kSlices / 2];
-#pragma unroll
-                        for (int d = 1; d < kSlices / 2; ++d) {
-                            hi = hi * (1 << kBits) + q[d];
-                            lo = lo * (1 << kBits) + q[kSlices / 2 + d];
-                        }
-                        const long long t = hi * (1ll << (kBits * kSlices / 2 - 12)) + ((lo + kLowRound) >> 12);
-                        // C = T 2^(E_i + F_j - 2W + 7 (S - 1) + 12)
-                        double v = 0.0;
-                        if (t != 0) v = scaled_double(t, ei + ej[x] - 2 * kWidth + kBits * (kSlices - 1) + 12);
-                        if (ei == kNonFinite || ej[x] == kNonFinite) v = __longlong_as_double(0x7FF8000000000000ll);
-                        ts[row * kTs + cl + x] = v;
-                    }
-                }
-                __syncthreads();
-                // each warp writes 16 rows; their old values and scales are loaded first
-                const int gj = j0 + 32 * h + lane;
-                constexpr int kRowsW = kBM / kNW;
-                const bool read_c = opt.subtract || s0 > 0;
-                const double csj = (opt.cs && gj < n) ? opt.cs[gj] : 1.0;
-                double old_c[kRowsW], rsv[kRowsW];
-#pragma unroll
-                for (int q = 0; q < kRowsW; ++q) {
-                    const int gi = i0 + w + q * kNW;
-                    const bool ok = gi < m && gj < n;
-                    old_c[q] = (ok && read_c) ? c[(size_t)gi * ldc + gj] : 0.0;
-                    rsv[q] = (ok && opt.rs) ? opt.rs[gi] : 1.0;
-                }
-#pragma unroll
-                for (int q = 0; q < kRowsW; ++q) {
-                    const int rr = w + q * kNW, gi = i0 + rr;
-                    if (gi >= m || gj >= n) continue;
-                    double v = ts[rr * kTs + lane];
-                    if (opt.rs) v = rsv[q] * v;
-                    if (opt.cs) v = v * csj;
-                    c[(size_t)gi * ldc + gj] = opt.subtract ? old_c[q] - v : (s0 == 0 ? v : old_c[q] + v);
-                }
-                // generic accesses to the stage are ordered before later bulk copies into it
-                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                __syncthreads();
-            }
-            // every warp has read the accumulators before the next MMAs overwrite them
-            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-            __syncthreads();
-            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            if (ws.cycles && threadIdx.x == 0) ws.cycles[2] += clock64() - te;
         }
+        if (*fail) {
+            // no copy may still be landing when the CTA moves on: wait (bounded) for the
+            // last `stages` steps this thread issued
+            for (uint32_t q = (g > step0 + stages ? g - stages : step0); q < g; ++q)
+                bar_wait(&tc->full[q % stages], (q / stages) & 1);
+        }
+    } else if (w == 0 && lane == 0) {
+        // MMA issue: per k step A_t times the stacked B_0 .. B_{7-t} (diagonals t .. 7 are the
+        // contiguous columns [32 t, 256) of the unit's accumulator buffer), one MMA per t
+        uint32_t g = step0;
+        for (int u = 0; u < n_units && !*fail; ++u) {
+            int tm, tn, c0, cs;
+            unit_of(u, tm, tn, c0, cs);
+            const uint32_t U = unit0 + u, b = U & 1, ub = U >> 1;
+            if (ub >= 1 && !bar_wait(&tc->acc_empty[b], (ub - 1) & 1, fail)) { *fail = 1; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t acc = tmem + b * kAccCols;
+            bool ok = true;
+            for (int s = 0; s < cs; ++s, ++g) {
+                const int i = g % stages;
+                if (!bar_wait(&tc->full[i], (g / stages) & 1, fail)) { ok = false; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t st = smem_u32(stage + (size_t)i * kStageBytes);
+#pragma unroll
+                for (int t = 0; t < kSlices; ++t)
+                    mma(acc + (uint32_t)(t * kBN), smem_desc(st + t * kTileA * 2), smem_desc(st + kStepA * 2),
+                        idesc((kSlices - t) * kBN), (s > 0 || t > 0) ? 1u : 0u);
+                commit(&tc->empty[i]);
+            }
+            if (!ok) { *fail = 1; break; }
+            commit(&tc->acc_full[b]);
+        }
+    } else if (w >= kEpiWarp0) {
+        // epilogue: warp w drains TMEM lanes 32 (w % 4) .. of the unit's buffer (its 32 rows of
+        // the tile), 8 columns at a time: all 8 diagonals read before one wait, combined in
+        // int64, converted to float64 with integer operations and written straight to C
+        const int quad = w & 3;
+        long long epi_cycles = 0;
+        for (int u = 0; u < n_units; ++u) {
+            int tm, tn, c0, cs;
+            unit_of(u, tm, tn, c0, cs);
+            const uint32_t U = unit0 + u, b = U & 1, ub = U >> 1;
+            const int i0 = tm * kBM, j0 = tn * kBN;
+            const int gi = i0 + 32 * quad + lane;          // this thread's row of C
+            const bool row_ok = gi < m;
+            const bool read_c = opt.subtract || c0 > 0;
+            if (read_c && row_ok) {   // the row's old values, requested into L2 while the MMAs run
+                asm volatile("prefetch.L2 [%0];\n" :: "l"(c + (size_t)gi * ldc + j0));
+                if (j0 + 16 < n) asm volatile("prefetch.L2 [%0];\n" :: "l"(c + (size_t)gi * ldc + j0 + 16));
+            }
+            // every lane waits; the outcome is made uniform over the warp before the collective
+            // TMEM loads
+            const bool bad = __any_sync(0xffffffffu, !bar_wait(&tc->acc_full[b], ub & 1, fail));
+            if (bad) {
+                if (lane == 0) *fail = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const long long te = clock64();
+            const int ei = row_ok ? ea[gi] : 0;
+            const double rsv = (row_ok && opt.rs) ? opt.rs[gi] : 1.0;
+            // |D_d| <= 8 k 64^2 < 2^22 for the k of this chunk
+            const bool magic_ok = cs * kBK * 8 * 64 * 64 < (1 << 22);
+            const uint32_t acc = tmem + ((uint32_t)(32 * quad) << 16) + b * kAccCols;
+            // 8 old values of C per group, the next group's loaded while this one is combined;
+            // 16-byte accesses where the row segment is aligned (ldc even, 16-byte base)
+            double* const crow0 = c + (size_t)gi * ldc + j0;
+            const bool vec = (((uintptr_t)crow0 & 15) == 0) && (ldc % 2 == 0);
+            auto load8 = [&](int jc, double (&o)[8]) {
+                const double* p = c + (size_t)gi * ldc + jc;
+                if (vec && jc + 8 <= n) {
+#pragma unroll
+                    for (int x = 0; x < 8; x += 2) {
+                        const double2 v = *reinterpret_cast<const double2*>(p + x);
+                        o[x] = v.x;
+                        o[x + 1] = v.y;
+                    }
+                } else {
+#pragma unroll
+                    for (int x = 0; x < 8; ++x) o[x] = (jc + x < n) ? p[x] : 0.0;
+                }
+            };
+            double old[8], old_next[8];
+            if (read_c && row_ok) load8(j0, old);
+#pragma unroll 1
+            for (int grp = 0; grp < kBN / 8; ++grp) {
+                const int jc = j0 + 8 * grp;
+                if (jc >= n) break;   // uniform: columns beyond C (the rows differ per lane)
+                uint32_t r[kSlices][8];
+#pragma unroll
+                for (int d = 0; d < kSlices; ++d) tmem_ld8(acc + (uint32_t)(d * kBN + 8 * grp), r[d]);
+                if (read_c && row_ok && grp + 1 < kBN / 8 && jc + 8 < n) load8(jc + 8, old_next);
+                tmem_wait();
+                if (!row_ok) continue;
+                double* crow = c + (size_t)gi * ldc + jc;
+                double outv[8];
+#pragma unroll
+                for (int x = 0; x < 8; ++x) {
+                    outv[x] = 0.0;
+                    if (jc + x >= n) continue;
+                    // T = sum_d D_d 2^(7 (7 - d)) / 2^12 from two Horner halves (|D_d| <= 2^24,
+                    // each half < 2^46); the 12 dropped low bits are 2^-60 of the largest sum.
+                    // The exact FP32 integers to int32: below 2^22 by the 1.5 2^23 magic
+                    // number on the FMA / ALU pipes, else by F2I on the XU pipe
+                    int q[kSlices];
+                    if (magic_ok) {
+#pragma unroll
+                        for (int d = 0; d < kSlices; ++d)
+                            q[d] = __float_as_int(__uint_as_float(r[d][x]) + 12582912.0f) - 0x4B400000;
+                    } else {
+#pragma unroll
+                        for (int d = 0; d < kSlices; ++d) q[d] = __float2int_rn(__uint_as_float(r[d][x]));
+                    }
+                    long long hi = q[0], lo = q[kSlices / 2];
+#pragma unroll
+                    for (int d = 1; d < kSlices / 2; ++d) {
+                        hi = hi * (1 << kBits) + q[d];
+                        lo = lo * (1 << kBits) + q[kSlices / 2 + d];
+                    }
+                    const long long tt = hi * (1ll << (kBits * kSlices / 2 - 12)) + ((lo + kLowRound) >> 12);
+                    const int ej = eb[jc + x];
+                    // C = T 2^(E_i + F_j - 2W + 7 (S - 1) + 12)
+                    double v = 0.0;
+                    if (tt != 0) v = scaled_double(tt, ei + ej - 2 * kWidth + kBits * (kSlices - 1) + 12);
+                    if (ei == kNonFinite || ej == kNonFinite) v = __longlong_as_double(0x7FF8000000000000ll);
+                    if (opt.rs) v = rsv * v;
+                    if (opt.cs) v = v * opt.cs[jc + x];
+                    outv[x] = opt.subtract ? old[x] - v : (c0 == 0 ? v : old[x] + v);
+                }
+                if (vec && jc + 8 <= n) {
+#pragma unroll
+                    for (int x = 0; x < 8; x += 2)
+                        *reinterpret_cast<double2*>(crow + x) = make_double2(outv[x], outv[x + 1]);
+                } else {
+#pragma unroll
+                    for (int x = 0; x < 8; ++x)
+                        if (jc + x < n) crow[x] = outv[x];
+                }
+#pragma unroll
+                for (int x = 0; x < 8; ++x) old[x] = old_next[x];
+            }
+            // every lane has read its accumulators before the buffer is handed back
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) bar_arrive(&tc->acc_empty[b]);
+            epi_cycles += clock64() - te;
+        }
+        if (ws.cycles && w == kEpiWarp0 && lane == 0) ws.cycles[2] += epi_cycles;
     }
-    if (ws.cycles && threadIdx.x == 0) ws.cycles[1] += clock64() - t1;
+    // every role is done: C is written, the MMAs have completed (each unit's epilogue waited
+    // for its commit), the copies have landed
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (threadIdx.x == 0) {
+        uint32_t steps = 0;
+        for (int u = 0; u < n_units; ++u) {
+            int tm, tn, c0, cs;
+            unit_of(u, tm, tn, c0, cs);
+            steps += cs;
+        }
+        tc->steps = step0 + steps;
+        tc->units = unit0 + n_units;
+        if (ws.cycles) ws.cycles[1] += clock64() - t1;
+    }
+    __syncthreads();
 }
 
 template <bool TA, bool TB>

@@ -135,9 +135,11 @@ template <typename T> __device__ __forceinline__ double* slot_d(const TSmem<T>& 
     return reinterpret_cast<double*>(slot_U(sm, idx, nn) + 2 * nn);
 }
 
-// Product categories whose emulated GEMMs are inlined at their call sites: the most frequent
-// ones (the per-slice wraps, the delayed-update flushes and the B-chain products, seven call
-// sites); every other site calls the single out-of-line copy.
+// Product categories whose emulated GEMMs are inlined at their call sites (a mask of
+// LQMC_FP64E_NATIVE_* bits): the most frequent ones (the wraps -- inside the out-of-line
+// wrap_t --, the delayed-update flushes and the B-chain products); every other site calls the
+// single out-of-line copy.  Calling out of line from the kernel body makes it keep more live
+// values across calls (255 registers and spills with no category inlined, none with these).
 #ifndef LQMC_OZ_INLINE_CATS
 #define LQMC_OZ_INLINE_CATS (LQMC_FP64E_NATIVE_WRAP | LQMC_FP64E_NATIVE_UPDATE | LQMC_FP64E_NATIVE_STACK)
 #endif
@@ -634,16 +636,39 @@ __device__ double green_udt_t(const ChainDesc& d, TSmem<T>& sm, const T* ur, con
     double la, sw;
     int sing;
     const long long t0 = clock64();
-    lu_solve_dispatch<T, EMU>(sm, n, &la, &sw, &sing);
+    double* zz = sm.s1;   // Z = M^-1 D_Rb^-1 U_R^T
+    bool by_inverse = false;
+    if constexpr (EMU) by_inverse = !(sm.native & LQMC_FP64E_NATIVE_LU_RHS);
+    if (by_inverse) {
+        // With emulated products the right-hand side D_Rb^-1 U_R^T (rows graded by 1 / dbr,
+        // down to ~1e-30) is not pushed through the substitutions, whose intermediate rows
+        // would cancel against the fixed-point rounding of their larger neighbours.  M itself
+        // is O(1) and well conditioned: its inverse comes from the LU with an identity
+        // right-hand side, and Z = M^-1 (D_Rb^-1 U_R^T) is one product in which every term
+        // of an output is at most its largest term.
+        T* rhs = sm.z1;
+        for (int i = warp_id(); i < n; i += kNW)
+            for (int j = lane; j < n; j += 32) {
+                const size_t e = (size_t)i * n + j;
+                rhs[e] = sm.s1[e];
+                sm.s1[e] = (i == j) ? 1.0 : 0.0;
+            }
+        __syncthreads();
+        lu_solve_dispatch<T, EMU>(sm, n, &la, &sw, &sing);
+        gemm_t<T, EMU, LQMC_FP64E_NATIVE_GREEN, false, false>(sm, sm.s0, n, sm.s1, n, (const T*)rhs, n, n, n, n);
+        zz = sm.s0;
+    } else {
+        lu_solve_dispatch<T, EMU>(sm, n, &la, &sw, &sing);
+    }
     if (threadIdx.x == 0) sm.sub[2] += clock64() - t0;
     if (sing) *singular = 1;
     double res = 0.0, m = 0.0;
     if (ul) {
         for (int i = warp_id(); i < n; i += kNW)
-            for (int j = lane; j < n; j += 32) sm.s1[(size_t)i * n + j] /= dbl[i];
+            for (int j = lane; j < n; j += 32) zz[(size_t)i * n + j] /= dbl[i];
         __syncthreads();
         // G = U_L Z: A(i,p) = U_L[i][p] = ul[p n + i]
-        gemm_t<T, EMU, LQMC_FP64E_NATIVE_GREEN, true, false>(sm, sm.z0, n, ul, n, sm.s1, n, n, n, n);
+        gemm_t<T, EMU, LQMC_FP64E_NATIVE_GREEN, true, false>(sm, sm.z0, n, ul, n, zz, n, n, n, n);
         for (int i = warp_id(); i < n; i += kNW)
             for (int j = lane; j < n; j += 32) {
                 const size_t e = (size_t)i * n + j;
@@ -654,8 +679,8 @@ __device__ double green_udt_t(const ChainDesc& d, TSmem<T>& sm, const T* ur, con
         for (int i = warp_id(); i < n; i += kNW)
             for (int j = lane; j < n; j += 32) {
                 const size_t e = (size_t)i * n + j;
-                if (residual) m = fmax(m, fabs(sm.s1[e] - (double)g[e]));
-                g[e] = (T)sm.s1[e];
+                if (residual) m = fmax(m, fabs(zz[e] - (double)g[e]));
+                g[e] = (T)zz[e];
             }
     }
     if (residual) res = block_max(m, sm.sv);
