@@ -639,7 +639,9 @@ __device__ double green_udt_t(const ChainDesc& d, TSmem<T>& sm, const T* ur, con
     double* zz = sm.s1;   // Z = M^-1 D_Rb^-1 U_R^T
     bool by_inverse = false;
     if constexpr (EMU) by_inverse = !(sm.native & LQMC_FP64E_NATIVE_LU_RHS);
-    if (by_inverse) {
+    if constexpr (!EMU) {
+        lu_solve_dispatch<T, EMU>(sm, n, &la, &sw, &sing);
+    } else if (by_inverse) {
         // With emulated products the right-hand side D_Rb^-1 U_R^T (rows graded by 1 / dbr,
         // down to ~1e-30) is not pushed through the substitutions, whose intermediate rows
         // would cancel against the fixed-point rounding of their larger neighbours.  M itself
