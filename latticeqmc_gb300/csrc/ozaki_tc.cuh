@@ -12,7 +12,8 @@
 // systematically over k.  Each A_t B_u is a tcgen05.mma (kind::f16, BF16 x BF16 -> FP32,
 // M = 128, K = 16) accumulating into the TMEM columns of diagonal d: the eight accumulators
 // of a 128 x 32 output tile take 256 TMEM columns, two tiles the SM's 512.  The FP32 sums are exact
-// integers while |D_d| <= 8 k 64^2 <= 2^24, i.e. for k <= kMaxK = 512; longer products are cut
+// integers while |D_d| <= 8 k 64^2 <= 2^23, i.e. for k <= kMaxK = 256 (the bound that also lets
+// the epilogue combine digit pairs in int32); longer products are cut
 // into chunks of kMaxK whose results are added in float64.  A row (column) holding a NaN or
 // Inf gives NaN in its output row (column).
 //
@@ -55,7 +56,8 @@ constexpr int kTileA = kBM * kBK;             // bf16 elements of one slice tile
 constexpr int kTileB = kBN * kBK;             // one slice tile of B (1 KB)
 constexpr int kStepA = kSlices * kTileA;      // all slices of one (row block, k step)
 constexpr int kStepB = kSlices * kTileB;
-constexpr int kMaxK = 512;                    // exact FP32 diagonal sums up to this k
+constexpr int kMaxK = 256;                    // exact FP32 diagonal sums (and the epilogue's
+                                              // int32 digit pairs) up to this k
 constexpr int kAccCols = kSlices * kBN;       // 256: the eight diagonals of one output tile
 constexpr int kTmemCols = 2 * kAccCols;       // 512: two accumulator buffers, the whole TMEM
 constexpr int kMaxStages = 3;                 // stage buffers of the copy / MMA ring
@@ -208,13 +210,14 @@ __device__ __forceinline__ int biased_exp(double v, int off) {
 __device__ __forceinline__ long long fixed55(double v, int e, int off) {
     const long long bits = __double_as_longlong(v);
     const int be = (int)((bits >> 52) & 0x7FF);
-    if (be == 0 || be == 0x7FF || e == kNonFinite) return 0;
+    const bool zero = be == 0 || be == 0x7FF || e == kNonFinite;
     const unsigned long long mant = ((unsigned long long)bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    // v 2^(55 - e) = mant 2^(be - 1075 + 55 - e); |v| < 2^e bounds the left shift by 2
+    // v 2^(55 - e) = mant 2^(be - 1075 + 55 - e); |v| < 2^e bounds the left shift by 2.
+    // Selects only (both shifts clamped to [0, 63]), so that the 8 elements of a unit interleave
     const int rs = 1075 - 55 + e - (be + off);
-    unsigned long long mag;
-    if (rs <= 0) mag = mant << (-rs);
-    else mag = (rs < 64) ? ((mant >> (rs - 1)) + 1ull) >> 1 : 0ull;
+    const unsigned long long left = mant << min(max(-rs, 0), 63);
+    const unsigned long long right = ((mant >> (min(max(rs, 1), 64) - 1)) + 1ull) >> 1;
+    const unsigned long long mag = zero ? 0ull : (rs <= 0 ? left : right);
     return bits < 0 ? -(long long)mag : (long long)mag;
 }
 
@@ -238,7 +241,7 @@ static_assert((kScratchStripes + 8 * kNT) * sizeof(int) <= (kStepA + kStepB) * s
 // requests are in flight.
 // kshift (optional, k ints): element (r, q) is split as X(r, q) 2^kshift[q] (exact).
 template <int BLK>
-__device__ void split_tiles(const double* x, int ld, bool trans, int rows, int k, int* exps,
+__device__ __noinline__ void split_tiles(const double* x, int ld, bool trans, int rows, int k, int* exps,
                             __nv_bfloat16* dst, int* scratch, const int* kshift = nullptr) {
     const int kp = kpad(k), S = kp / kBK, rp = rows_pad(rows, BLK);
     if (!trans) {
@@ -320,11 +323,11 @@ __device__ void split_tiles(const double* x, int ld, bool trans, int rows, int k
             for (int c = 0; c < 4; ++c) {
                 const uint32_t a0 = ((t < 4 ? fhi[2 * c] : flo[2 * c]) >> sh) & mask;
                 const uint32_t a1 = ((t < 4 ? fhi[2 * c + 1] : flo[2 * c + 1]) >> sh) & mask;
-                // field - 64 exactly in float (2^23 magic) and in bfloat16
+                // field - 64 exactly in float (2^23 magic); at most 7 significant bits, so
+                // its bfloat16 is the float's upper half: one byte permute packs two
                 const float f0 = __uint_as_float(0x4B000000u | a0) - 8388672.0f;
                 const float f1 = __uint_as_float(0x4B000000u | a1) - 8388672.0f;
-                const __nv_bfloat162 p = __floats2bfloat162_rn(f0, f1);
-                w[c] = *reinterpret_cast<const uint32_t*>(&p);
+                w[c] = __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632);
             }
             *reinterpret_cast<uint4*>(base + (size_t)t * (BLK * kBK)) = make_uint4(w[0], w[1], w[2], w[3]);
         }
@@ -433,17 +436,14 @@ __device__ __forceinline__ void tmem_wait() {
 // The epilogue stays off the float64 pipe (a few operations per clock per SM on this part)
 // and keeps its integer work short and branch-free.
 
-// t * 2^s as float64, rounded to nearest-even, t != 0, |t| < 2^63
+// t * 2^s as float64, t != 0, |t| < 2^63: t rounded to 53 significant bits half away from
+// zero (the 12 bits below t were already dropped, so ties carry no meaning), then scaled.
 __device__ __forceinline__ double scaled_double(long long t, int s) {
     const unsigned long long sign = (unsigned long long)t & (1ull << 63);
     const unsigned long long a = t < 0 ? (unsigned long long)(-t) : (unsigned long long)t;
     const int nb = 64 - __clzll((long long)a);              // bit length, 1 .. 63
-    const int sh = nb - 53;                                  // > 0: bits to round away
-    const int shr = sh > 0 ? sh : 0, shl = sh > 0 ? 0 : -sh;
-    unsigned long long mant = (a >> shr) << shl;
-    const unsigned long long rem = a & ((1ull << shr) - 1ull);
-    const unsigned long long half = sh > 0 ? (1ull << (shr - 1)) : 1ull;
-    mant += (rem > half || (rem == half && (mant & 1ull))) ? 1ull : 0ull;
+    const int shr = max(nb - 53, 0), shl = max(53 - nb, 0);
+    const unsigned long long mant = ((a + ((1ull << shr) >> 1)) >> shr) << shl;
     const int be = nb - 1 + 1023 + s;
     if (be > 0 && be < 0x7FF - 1)
         // a rounding carry to 2^53 moves into the exponent field
@@ -454,7 +454,150 @@ __device__ __forceinline__ double scaled_double(long long t, int s) {
     return ldexp(unit, s);
 }
 
+// The same conversion without branches for the result of one output: t * 2^s when it is a
+// normal float64 (or 0 for t == 0); `special` is set when it is subnormal or overflows, to be
+// redone with scaled_double.  Every operation is a select, so eight outputs interleave.
+__device__ __forceinline__ double scaled_double_normal(long long t, int s, bool& special) {
+    const unsigned long long sign = (unsigned long long)t & (1ull << 63);
+    const unsigned long long a = t < 0 ? (unsigned long long)(-t) : (unsigned long long)t;
+    const int nb = 64 - __clzll((long long)a);              // bit length, 0 .. 63
+    const int shr = max(nb - 53, 0), shl = max(53 - nb, 0);
+    const unsigned long long mant = ((a + ((1ull << shr) >> 1)) >> shr) << shl;
+    const int be = nb - 1 + 1023 + s;
+    special = (a != 0) && !(be > 0 && be < 0x7FF - 1);
+    const long long bits = (long long)(sign | (((unsigned long long)be << 52) + (mant - (1ull << 52))));
+    return a == 0 ? 0.0 : __longlong_as_double(bits);
+}
+
 // ---- the product -------------------------------------------------------------------------
+
+// The fixed-point sums of 8 outputs of one row from their 8 diagonal accumulators r[d][x]
+// (exact FP32 integers): T = sum_d D_d 2^(7 (7 - d)) / 2^12.  D_d sums d + 1 digit pairs of
+// |q| <= 64 over the chunk's k, so |D_d| <= (d + 1) k 2^12: the first MAGIC diagonals are
+// below 2^22 and convert by the 1.5 2^23 magic number on the FMA / ALU pipes, the others by
+// F2I on the XU pipe.  Digit pairs combine in int32 (128 D + D' < 2^31 for k <= 256), then
+// two int64 halves (each < 2^45); the 12 dropped low bits are 2^-60 of the largest sum.
+// Straight-line code over the 8 outputs: their dependency chains interleave.
+template <int MAGIC>
+__device__ __forceinline__ void fixed_sums(const uint32_t (&r)[kSlices][8], long long (&tt)[8]) {
+#pragma unroll
+    for (int x = 0; x < 8; ++x) {
+        int q[kSlices];
+#pragma unroll
+        for (int d = 0; d < kSlices; ++d)
+            q[d] = d < MAGIC ? __float_as_int(__uint_as_float(r[d][x]) + 12582912.0f) - 0x4B400000
+                             : __float2int_rn(__uint_as_float(r[d][x]));
+        const int p0 = q[0] * (1 << kBits) + q[1];
+        const int p1 = q[2] * (1 << kBits) + q[3];
+        const int p2 = q[4] * (1 << kBits) + q[5];
+        const int p3 = q[6] * (1 << kBits) + q[7];
+        const long long hi = (long long)p0 * (1 << (2 * kBits)) + p1;
+        const long long lo = (long long)p2 * (1 << (2 * kBits)) + p3;
+        tt[x] = hi * (1ll << (kBits * kSlices / 2 - 12)) + ((lo + kLowRound) >> 12);
+    }
+}
+
+// The drain of one unit by one epilogue warp: its 32 rows (this lane: row gi) of the 128 x 32
+// tile whose accumulators start at TMEM address `acc` (lane quadrant included), 8 columns at a
+// time: all 8 diagonals read before one wait, combined in int32 / int64, converted to float64
+// with integer operations (t 2^s, t rounded to 53 bits half away from zero) and written to C.
+// Each step is branch-free over the 8 outputs (the rare subnormal / overflowing results are
+// redone after one test of the group), so that the single warp of each SM sub-partition has
+// 8 independent chains to issue from.  Out of line: its many live registers stay out of the
+// kernels that call the product inline.
+static __device__ __noinline__ void drain_tile(double* c, int ldc, int m, int n, int gi, int j0, int c0,
+                                               int cs, const int* ea, const int* eb, GemmOpt<double> opt,
+                                               uint32_t acc) {
+    const int lane = lane_id();
+    const bool row_ok = gi < m;
+    const bool read_c = opt.subtract || c0 > 0;
+    const int ei = row_ok ? ea[gi] : 0;
+    const double rsv = (row_ok && opt.rs) ? opt.rs[gi] : 1.0;
+    // the tile's 32 column exponents (and column scales): one per lane, broadcast by shuffles
+    const int jl = min(j0 + lane, n - 1);
+    const int ej_lane = eb[jl];
+    const double cs_lane = opt.cs ? opt.cs[jl] : 1.0;
+    const int sbase = ei - 2 * kWidth + kBits * (kSlices - 1) + 12;
+    const bool all_magic = cs * kBK <= kMaxK / 2;       // (7 + 1) k 2^12 <= 2^22
+    static_assert(kMaxK <= 256, "int32 digit pairs and 4 magic-number diagonals assume k <= 256");
+    double* const crow0 = c + (size_t)gi * ldc + j0;
+    const bool vec = (((uintptr_t)crow0 & 15) == 0) && (ldc % 2 == 0);
+#pragma unroll 1
+    for (int grp = 0; grp < kBN / 8; ++grp) {
+        const int jc = j0 + 8 * grp;
+        if (jc >= n) break;   // uniform: columns beyond C (the rows differ per lane)
+        uint32_t r[kSlices][8];
+#pragma unroll
+        for (int d = 0; d < kSlices; ++d) tmem_ld8(acc + (uint32_t)(d * kBN + 8 * grp), r[d]);
+        double* crow = c + (size_t)gi * ldc + jc;
+        const bool full8 = jc + 8 <= n;
+        double old[8];
+#pragma unroll
+        for (int x = 0; x < 8; ++x) old[x] = 0.0;
+        if (read_c && row_ok) {
+            if (vec && full8) {
+#pragma unroll
+                for (int x = 0; x < 8; x += 2) {
+                    const double2 v = *reinterpret_cast<const double2*>(crow + x);
+                    old[x] = v.x;
+                    old[x + 1] = v.y;
+                }
+            } else {
+#pragma unroll
+                for (int x = 0; x < 8; ++x) old[x] = (jc + x < n) ? crow[x] : 0.0;
+            }
+        }
+        int sx[8];
+#pragma unroll
+        for (int x = 0; x < 8; ++x) sx[x] = __shfl_sync(0xffffffffu, ej_lane, 8 * grp + x);
+        tmem_wait();
+        long long tt[8];
+        if (all_magic) fixed_sums<kSlices>(r, tt);
+        else fixed_sums<kSlices / 2>(r, tt);
+        double v[8];
+        unsigned special = 0, nonfinite = 0;
+#pragma unroll
+        for (int x = 0; x < 8; ++x) {
+            bool sp;
+            v[x] = scaled_double_normal(tt[x], sbase + sx[x], sp);
+            special |= (unsigned)sp << x;
+            nonfinite |= (unsigned)(sx[x] == kNonFinite) << x;
+        }
+        if (ei == kNonFinite) nonfinite = 0xFFu;
+        if (special | nonfinite) {   // rare: subnormal or overflowing results, NaN rows / columns
+#pragma unroll 1
+            for (int x = 0; x < 8; ++x) {
+                if ((special >> x) & 1u) v[x] = scaled_double(tt[x], sbase + sx[x]);
+                if ((nonfinite >> x) & 1u) v[x] = __longlong_as_double(0x7FF8000000000000ll);
+            }
+        }
+        if (opt.rs) {
+#pragma unroll
+            for (int x = 0; x < 8; ++x) v[x] *= rsv;
+        }
+        if (opt.cs) {
+#pragma unroll
+            for (int x = 0; x < 8; ++x) v[x] *= __shfl_sync(0xffffffffu, cs_lane, 8 * grp + x);
+        }
+        if (opt.subtract) {
+#pragma unroll
+            for (int x = 0; x < 8; ++x) v[x] = old[x] - v[x];
+        } else if (c0 > 0) {
+#pragma unroll
+            for (int x = 0; x < 8; ++x) v[x] = old[x] + v[x];
+        }
+        if (!row_ok) continue;
+        if (vec && full8) {
+#pragma unroll
+            for (int x = 0; x < 8; x += 2)
+                *reinterpret_cast<double2*>(crow + x) = make_double2(v[x], v[x + 1]);
+        } else {
+#pragma unroll
+            for (int x = 0; x < 8; ++x)
+                if (jc + x < n) crow[x] = v[x];
+        }
+    }
+}
 
 // C (m x n, ldc) = op(A) op(B) with float64 accuracy; epilogue as blk::tile_gemm (row /
 // column scale, subtract).  A(i, p) = TA ? a[p lda + i] : a[i lda + p];
@@ -619,88 +762,8 @@ __device__ __forceinline__ void oz_gemm_tc_impl(double* c, int ldc, const double
             }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
             const long long te = clock64();
-            const int ei = row_ok ? ea[gi] : 0;
-            const double rsv = (row_ok && opt.rs) ? opt.rs[gi] : 1.0;
-            // |D_d| <= 8 k 64^2 < 2^22 for the k of this chunk
-            const bool magic_ok = cs * kBK * 8 * 64 * 64 < (1 << 22);
-            const uint32_t acc = tmem + ((uint32_t)(32 * quad) << 16) + b * kAccCols;
-            // 8 old values of C per group, the next group's loaded while this one is combined;
-            // 16-byte accesses where the row segment is aligned (ldc even, 16-byte base)
-            double* const crow0 = c + (size_t)gi * ldc + j0;
-            const bool vec = (((uintptr_t)crow0 & 15) == 0) && (ldc % 2 == 0);
-            auto load8 = [&](int jc, double (&o)[8]) {
-                const double* p = c + (size_t)gi * ldc + jc;
-                if (vec && jc + 8 <= n) {
-#pragma unroll
-                    for (int x = 0; x < 8; x += 2) {
-                        const double2 v = *reinterpret_cast<const double2*>(p + x);
-                        o[x] = v.x;
-                        o[x + 1] = v.y;
-                    }
-                } else {
-#pragma unroll
-                    for (int x = 0; x < 8; ++x) o[x] = (jc + x < n) ? p[x] : 0.0;
-                }
-            };
-            double old[8], old_next[8];
-            if (read_c && row_ok) load8(j0, old);
-#pragma unroll 1
-            for (int grp = 0; grp < kBN / 8; ++grp) {
-                const int jc = j0 + 8 * grp;
-                if (jc >= n) break;   // uniform: columns beyond C (the rows differ per lane)
-                uint32_t r[kSlices][8];
-#pragma unroll
-                for (int d = 0; d < kSlices; ++d) tmem_ld8(acc + (uint32_t)(d * kBN + 8 * grp), r[d]);
-                if (read_c && row_ok && grp + 1 < kBN / 8 && jc + 8 < n) load8(jc + 8, old_next);
-                tmem_wait();
-                if (!row_ok) continue;
-                double* crow = c + (size_t)gi * ldc + jc;
-                double outv[8];
-#pragma unroll
-                for (int x = 0; x < 8; ++x) {
-                    outv[x] = 0.0;
-                    if (jc + x >= n) continue;
-                    // T = sum_d D_d 2^(7 (7 - d)) / 2^12 from two Horner halves (|D_d| <= 2^24,
-                    // each half < 2^46); the 12 dropped low bits are 2^-60 of the largest sum.
-                    // The exact FP32 integers to int32: below 2^22 by the 1.5 2^23 magic
-                    // number on the FMA / ALU pipes, else by F2I on the XU pipe
-                    int q[kSlices];
-                    if (magic_ok) {
-#pragma unroll
-                        for (int d = 0; d < kSlices; ++d)
-                            q[d] = __float_as_int(__uint_as_float(r[d][x]) + 12582912.0f) - 0x4B400000;
-                    } else {
-#pragma unroll
-                        for (int d = 0; d < kSlices; ++d) q[d] = __float2int_rn(__uint_as_float(r[d][x]));
-                    }
-                    long long hi = q[0], lo = q[kSlices / 2];
-#pragma unroll
-                    for (int d = 1; d < kSlices / 2; ++d) {
-                        hi = hi * (1 << kBits) + q[d];
-                        lo = lo * (1 << kBits) + q[kSlices / 2 + d];
-                    }
-                    const long long tt = hi * (1ll << (kBits * kSlices / 2 - 12)) + ((lo + kLowRound) >> 12);
-                    const int ej = eb[jc + x];
-                    // C = T 2^(E_i + F_j - 2W + 7 (S - 1) + 12)
-                    double v = 0.0;
-                    if (tt != 0) v = scaled_double(tt, ei + ej - 2 * kWidth + kBits * (kSlices - 1) + 12);
-                    if (ei == kNonFinite || ej == kNonFinite) v = __longlong_as_double(0x7FF8000000000000ll);
-                    if (opt.rs) v = rsv * v;
-                    if (opt.cs) v = v * opt.cs[jc + x];
-                    outv[x] = opt.subtract ? old[x] - v : (c0 == 0 ? v : old[x] + v);
-                }
-                if (vec && jc + 8 <= n) {
-#pragma unroll
-                    for (int x = 0; x < 8; x += 2)
-                        *reinterpret_cast<double2*>(crow + x) = make_double2(outv[x], outv[x + 1]);
-                } else {
-#pragma unroll
-                    for (int x = 0; x < 8; ++x)
-                        if (jc + x < n) crow[x] = outv[x];
-                }
-#pragma unroll
-                for (int x = 0; x < 8; ++x) old[x] = old_next[x];
-            }
+            drain_tile(c, ldc, m, n, gi, j0, c0, cs, ea, eb, opt,
+                       tmem + ((uint32_t)(32 * quad) << 16) + b * kAccCols);
             // every lane has read its accumulators before the buffer is handed back
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
             __syncwarp();

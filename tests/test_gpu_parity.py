@@ -22,10 +22,12 @@ pytestmark = pytest.mark.gpu
 
 # max|G_gpu - G_reference| per sweep allowed in compat mode.  The reference wraps G the
 # "upward" way while sweeping down (lqmc.py:337-345) without stabilisation, so rounding
-# differences grow within a sweep; these floors are what a float64 restatement with a
-# different summation order reaches (a numpy shadow of the same math lands at the same
-# order of magnitude: 4.6e-9 on 2x2, 1.1e-2 on 4x4, 9.6e-5 on 8x8).
-COMPAT_G_FLOOR = {2: 1e-5, 4: 5e-2, 8: 1e-3}
+# differences grow within a sweep and spike where an update is near-singular.  The largest
+# differences this kernel reaches over the recorded runs are 5.6e-6 (2x2, 40 sweeps),
+# 1.1e-5 (4x4) and 9.6e-7 (8x8); the floors are about ten times those.  (A numpy shadow of the
+# same math with another summation order has reached 4.6e-9, 1.1e-2 and 9.6e-5: the
+# amplification, not the kernel, sets the scale.)
+COMPAT_G_FLOOR = {2: 5e-5, 4: 1e-4, 8: 1e-5}
 
 
 @pytest.mark.parametrize("side", [2, 4, 8])

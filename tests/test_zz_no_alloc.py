@@ -39,18 +39,22 @@ def _dev(torch, a, dtype):
     return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype).cuda()
 
 
-def test_static_sweep_matches_engine_on_two_calls():
+def _static_case(side, L, stab, replay, seed=11):
+    """Two lqmc_sweep_static calls of two sweeps each on buffers the test owns, each checked
+    against the same chain swept by Engine (lqmc_sweep) from the same inputs."""
     torch = pytest.importorskip("torch")
     lib = _native.load()
-    side, U, beta, L, stab, seed = 4, 4.0, 2.0, 20, 5, 11
+    U, beta = 4.0, 2.0
     m = HubbardModel(u=U, t=1, mu=0)
     m.build_square(side)
     K = m.ham_kinetic()
     N = side * side
-    field = (2 * np.random.default_rng(3).integers(0, 2, (N, L)) - 1).astype(np.int8)
+    rng = np.random.default_rng(seed)
+    field = (2 * rng.integers(0, 2, (N, L)) - 1).astype(np.int8)
     spec = ChainSpec(K, U, beta, L, field)
     eki = expm(spec.dtau * K)
-    eng = Engine([spec], mode="dqmc", rng="philox", seed=seed, stab_every=stab)
+    eng = Engine([spec], mode="dqmc", rng="replay" if replay else "philox", seed=seed,
+                 stab_every=stab)
 
     # the caller's own device buffers (allocated here, by the caller, not by the library)
     bufs = {
@@ -67,30 +71,52 @@ def test_static_sweep_matches_engine_on_two_calls():
         "status": torch.zeros(1, dtype=torch.int32, device="cuda"),
     }
     err = ctypes.create_string_buffer(256)
-    sc = StaticChain(n_sites=N, n_slices=L, stab_every=stab, rng=1, seed=seed, chain_id=0,
-                     measure=1, u=U, uniforms=None, error_message=ctypes.cast(err, ctypes.c_char_p),
-                     error_capacity=256)
+    sc = StaticChain(n_sites=N, n_slices=L, stab_every=stab, rng=0 if replay else 1, seed=seed,
+                     chain_id=0, measure=1, u=U, uniforms=None,
+                     error_message=ctypes.cast(err, ctypes.c_char_p), error_capacity=256)
     sc.exp_consts[:] = list(exp_constants(spec.lamb, N))
     for k, t in bufs.items():
         setattr(sc, k, t.data_ptr())
 
-    for call in range(2):
-        rc = lib.lqmc_sweep_static(ctypes.byref(sc), 2, None)
-        assert rc == 0, err.value
-        torch.cuda.synchronize()
-        eng.sweep(2, measure=True)
-        g_ref = eng.green(0)
-        gs_ref, cnt = eng.green_sum(0)
-        g = bufs["green"].cpu().numpy().reshape(2, N, N)
-        gs = bufs["green_sum"].cpu().numpy().reshape(2, N, N)
-        assert np.abs(g - g_ref).max() < 1e-10, f"call {call}"
-        assert np.abs(gs - gs_ref).max() < 1e-10, f"call {call}"
-        np.testing.assert_array_equal(bufs["field"].cpu().numpy().T, eng.field(0))
-        np.testing.assert_allclose(bufs["obs"].cpu().numpy(), eng.observables_raw(0), atol=1e-10)
-        d = bufs["diag"].cpu().numpy()
-        assert d[7] == 2 * (call + 1) and cnt == 2 * (call + 1)
-        assert int(bufs["status"].cpu().item()) == 0
-    eng.close()
+    try:
+        for call in range(2):
+            if replay:
+                u = rng.random(2 * N * L)
+                u_dev = _dev(torch, u, torch.float64)   # the caller's uniforms of this call
+                sc.uniforms = u_dev.data_ptr()
+                eng.set_uniforms(0, u)
+            rc = lib.lqmc_sweep_static(ctypes.byref(sc), 2, None)
+            assert rc == 0, err.value
+            torch.cuda.synchronize()
+            eng.sweep(2, measure=True)
+            g_ref = eng.green(0)
+            gs_ref, cnt = eng.green_sum(0)
+            g = bufs["green"].cpu().numpy().reshape(2, N, N)
+            gs = bufs["green_sum"].cpu().numpy().reshape(2, N, N)
+            assert np.abs(g - g_ref).max() < 1e-10, f"call {call}"
+            assert np.abs(gs - gs_ref).max() < 1e-10, f"call {call}"
+            np.testing.assert_array_equal(bufs["field"].cpu().numpy().T, eng.field(0))
+            np.testing.assert_allclose(bufs["obs"].cpu().numpy(), eng.observables_raw(0), atol=1e-10)
+            d = bufs["diag"].cpu().numpy()
+            assert d[7] == 2 * (call + 1) and cnt == 2 * (call + 1)
+            assert int(bufs["status"].cpu().item()) == 0
+    finally:
+        eng.close()
+
+
+def test_static_sweep_matches_engine_on_two_calls():
+    _static_case(4, 20, 5, replay=False)
+
+
+def test_static_sweep_replays_the_callers_uniforms_on_two_calls():
+    """LQMC_RNG_REPLAY: each call draws from the uniforms buffer the caller passes."""
+    _static_case(4, 20, 5, replay=True, seed=12)
+
+
+def test_static_sweep_at_the_largest_lattice_with_two_chunks():
+    """n_sites = LQMC_STATIC_MAX_SITES (8 x 8) with L = 2 stab_every: two chunks of slices,
+    the right-product stack of the scratch array in use."""
+    _static_case(8, 20, 10, replay=False, seed=13)
 
 
 def test_static_sweep_rejects_sizes_beyond_its_array():
