@@ -121,7 +121,7 @@ typedef struct lqmc_params {
     int32_t sweep_order;   /* LQMC_ORDER_*; LQMC_ORDER_ALTERNATE runs every chain on the tiled
                               kernel (LQMC_MODE_DQMC only)                                    */
     int32_t oz_stages;     /* LQMC_PREC_FP64E: stage buffers of the emulated GEMM's copy / MMA
-                              ring, 1 .. 3 (0: two, or one where two do not fit)             */
+                              ring, 1 .. 3 (0: three where they fit, else two, else one)     */
     int32_t reserved[1];
 } lqmc_params;
 

@@ -2,16 +2,22 @@
 
 For one workload shape (square lattice side, beta, L, precision) it times candidate settings of
 
-    stab_every   slices between stabilised refreshes of G
-    delay        depth k of the delayed rank-k updates (0: the engine's rule)
-    oz_stages    stage buffers of the emulated GEMM's copy / MMA ring (fp64e; 0: the rule)
-    sweep_order  'down' (the reference's order) or 'alternate'
+    stab_every    slices between stabilised refreshes of G
+    sweep_order   'down' (the reference's order) or 'alternate'
+    fp64e_native  (fp64e) product categories kept in native float64
+    delay         depth k of the delayed rank-k updates (0: the engine's rule)
+    oz_stages     stage buffers of the emulated GEMM's copy / MMA ring (fp64e; 0: the rule)
 
-on a few chains, checks each against the float64 engine run from identical fields and
-uniforms with the same stab_every and sweep order, and picks the fastest setting that meets
+on the workload's chain count, checks each against the float64 engine run from identical
+fields and uniforms with the same stab_every and sweep order (on fewer chains), and picks
+the fastest setting that meets
 
     max|G - G_fp64| <= tol after every compared sweep, identical accept/reject decisions, and
     no chain raising a status bit (LQMC_STATUS_DRIFT: a stabilisation residual above 1e-6).
+
+The search is two coordinate passes: a grid over the settings that decide accuracy
+(stab_every x sweep order x native categories) at the default delay and stage count, then
+every delay and stage count around the fastest passing grid point.
 
 Results go to a JSON cache keyed by the workload shape (``tuning/autotune.json`` beside this
 module); ``tuned(...)`` reads a record back.  Without a record the engine's own rules apply
@@ -46,9 +52,12 @@ def _specs(side, beta, L, chains, seed):
 
 def _engine(specs, precision, cand, device, rng, record=False):
     from .engine import Engine
+    kw = {}
+    if precision == "fp64e" and "fp64e_native" in cand:
+        kw["fp64e_native"] = tuple(cand["fp64e_native"])
     return Engine(specs, mode="dqmc", precision=precision, rng=rng, seed=1, record=record,
                   stab_every=cand["stab_every"], delay=cand.get("delay", 0), device=device,
-                  sweep_order=cand["sweep_order"], oz_stages=cand.get("oz_stages", 0))
+                  sweep_order=cand["sweep_order"], oz_stages=cand.get("oz_stages", 0), **kw)
 
 
 def time_candidate(specs, precision, cand, sweeps, device=0):
@@ -111,55 +120,93 @@ def check_candidate(specs, precision, cand, sweeps, device=0, ref_cache=None):
             "fp64_chains_flagged": int(np.count_nonzero(st_ref))}
 
 
-def default_candidates(precision, stabs=(6, 8, 10, 12, 16), delays=(8, 16, 32, 48),
-                       orders=("down", "alternate"), stages=(1, 2)):
-    """Every stab_every x sweep order at the engine's default delay and stages, every delay
-    and (fp64e) every stage count at stab 8 in both orders."""
-    cands = []
-    for order in orders:
-        for st in stabs:
-            cands.append({"stab_every": st, "delay": 0, "sweep_order": order, "oz_stages": 0})
-        for k in delays:
-            cands.append({"stab_every": 8, "delay": k, "sweep_order": order, "oz_stages": 0})
-        if precision == "fp64e":
-            for sg in stages:
-                cands.append({"stab_every": 8, "delay": 0, "sweep_order": order, "oz_stages": sg})
+# native-float64 category sets tried for fp64e: all emulated, the stabilised inverse's LU
+# (with or without its right-hand side) native, and the QR updates and B-chain products native
+# (the two categories whose emulation moves the stabilisation residual most)
+NATIVE_SETS = ((), ("lu",), ("lu", "lu_rhs"), ("udt", "stack"))
+
+
+def _dedup(cands):
     seen, out = set(), []
     for c in cands:
-        k = tuple(sorted(c.items()))
+        k = json.dumps(c, sort_keys=True)
         if k not in seen:
             seen.add(k)
             out.append(c)
     return out
 
 
-def autotune(side, beta, L, precision="fp64e", candidates=None, chains=8, time_sweeps=2,
-             acc_sweeps=3, tol=1e-6, device=0, cache=CACHE, log=print):
-    """Time and check every candidate; cache and return the record of the workload shape."""
-    if candidates is None:
-        candidates = default_candidates(precision)
-    specs = _specs(side, beta, L, chains, 4321)
-    ref_cache = {}
+def default_candidates(precision, stabs=(6, 8, 10, 12, 16), orders=("down", "alternate"),
+                       natives=NATIVE_SETS):
+    """The first pass: every stab_every x sweep order (x fp64e native set) at the engine's
+    default delay and stage count."""
+    nats = natives if precision == "fp64e" else (None,)
+    cands = []
+    for order in orders:
+        for nat in nats:
+            for st in stabs:
+                c = {"stab_every": st, "delay": 0, "sweep_order": order, "oz_stages": 0}
+                if nat is not None:
+                    c["fp64e_native"] = list(nat)
+                cands.append(c)
+    return _dedup(cands)
+
+
+def refine_candidates(best, precision, delays=(8, 16, 32, 48), stages=(1, 2, 3)):
+    """The second pass: each delay and (fp64e) each stage count around `best`."""
+    cands = [dict(best, delay=k) for k in delays]
+    if precision == "fp64e":
+        cands += [dict(best, oz_stages=sg) for sg in stages]
+    keys = ("stab_every", "delay", "sweep_order", "oz_stages", "fp64e_native")
+    return _dedup([{k: c[k] for k in keys if k in c} for c in cands])
+
+
+def _run(cands, specs_time, specs_acc, precision, time_sweeps, acc_sweeps, tol, device, ref_cache,
+         label, log):
     rows = []
-    for cand in candidates:
+    for cand in cands:
         t0 = time.perf_counter()
         try:
-            sec = time_candidate(specs, precision, cand, time_sweeps, device)
-            acc = check_candidate(specs, precision, cand, acc_sweeps, device, ref_cache)
+            sec = time_candidate(specs_time, precision, cand, time_sweeps, device)
+            acc = check_candidate(specs_acc, precision, cand, acc_sweeps, device, ref_cache)
             ok = acc["max_dG"] <= tol and acc["chains_flagged"] == 0 and acc["chains_diverged"] == 0
             row = dict(cand, seconds_per_sweep=sec, ok=ok, **acc)
         except RuntimeError as e:            # a setting the engine refuses (shared memory)
             row = dict(cand, ok=False, error=str(e))
         rows.append(row)
         if log:
-            log(f"autotune {shape_key(side, beta, L, precision)} {cand}: "
-                + (f"{row['seconds_per_sweep'] * 1e3:.1f} ms/sweep ({chains} chains), max|dG| "
-                   f"{row['max_dG']:.1e}, flagged {row['chains_flagged']}, diverged "
-                   f"{row['chains_diverged']}, {'ok' if row['ok'] else 'rejected'}"
+            log(f"autotune {label} {cand}: "
+                + (f"{row['seconds_per_sweep'] * 1e3:.1f} ms/sweep, max|dG| {row['max_dG']:.1e}, "
+                   f"flagged {row['chains_flagged']}, diverged {row['chains_diverged']}, "
+                   f"{'ok' if row['ok'] else 'rejected'}"
                    if "error" not in row else f"refused: {row['error']}")
                 + f" [{time.perf_counter() - t0:.0f}s]")
+    return rows
+
+
+def autotune(side, beta, L, precision="fp64e", candidates=None, chains=16, time_chains=64,
+             time_sweeps=2, acc_sweeps=4, tol=1e-6, device=0, cache=CACHE, log=print):
+    """Time and check the candidates (given, or the two passes above); cache and return the
+    record of the workload shape."""
+    label = shape_key(side, beta, L, precision)
+    specs_acc = _specs(side, beta, L, chains, 4321)
+    specs_time = _specs(side, beta, L, time_chains, 4321)
+    ref_cache = {}
+    args = (specs_time, specs_acc, precision, time_sweeps, acc_sweeps, tol, device, ref_cache, label, log)
+    if candidates is not None:
+        rows = _run(candidates, *args)
+    else:
+        rows = _run(default_candidates(precision), *args)
+        passing = sorted((r for r in rows if r["ok"]), key=lambda r: r["seconds_per_sweep"])
+        if passing:
+            best = {k: v for k, v in passing[0].items()
+                    if k in ("stab_every", "delay", "sweep_order", "oz_stages", "fp64e_native")}
+            done = {json.dumps({k: r[k] for k in best if k in r}, sort_keys=True) for r in rows}
+            extra = [c for c in refine_candidates(best, precision)
+                     if json.dumps(c, sort_keys=True) not in done]
+            rows += _run(extra, *args)
     passing = sorted((r for r in rows if r["ok"]), key=lambda r: r["seconds_per_sweep"])
-    record = {"shape": shape_key(side, beta, L, precision), "chains": chains, "tol": tol,
+    record = {"shape": label, "chains": chains, "time_chains": time_chains, "tol": tol,
               "time_sweeps": time_sweeps, "acc_sweeps": acc_sweeps,
               "chosen": passing[0] if passing else None,
               "runner_up": passing[1] if len(passing) > 1 else None, "candidates": rows}
@@ -186,9 +233,16 @@ def tuned(side, beta, L, precision, cache=CACHE):
 
 def settings(record):
     """Engine keyword arguments of a record's chosen setting."""
-    c = record["chosen"]
-    return {"stab_every": c["stab_every"], "delay": c["delay"], "sweep_order": c["sweep_order"],
-            "oz_stages": c["oz_stages"]}
+    return candidate_settings(record["chosen"])
+
+
+def candidate_settings(c):
+    """Engine keyword arguments of one candidate row."""
+    kw = {"stab_every": c["stab_every"], "delay": c["delay"], "sweep_order": c["sweep_order"],
+          "oz_stages": c["oz_stages"]}
+    if "fp64e_native" in c:
+        kw["fp64e_native"] = tuple(c["fp64e_native"])
+    return kw
 
 
 if __name__ == "__main__":
@@ -198,7 +252,8 @@ if __name__ == "__main__":
     ap.add_argument("--beta", type=float, default=8.0)
     ap.add_argument("--L", type=int, default=80)
     ap.add_argument("--precision", default="fp64e")
-    ap.add_argument("--chains", type=int, default=8)
+    ap.add_argument("--chains", type=int, default=16, help="chains of the accuracy check")
+    ap.add_argument("--time-chains", type=int, default=64, help="chains of the timing")
     a = ap.parse_args()
-    rec = autotune(a.side, a.beta, a.L, a.precision, chains=a.chains)
+    rec = autotune(a.side, a.beta, a.L, a.precision, chains=a.chains, time_chains=a.time_chains)
     print(json.dumps({k: rec[k] for k in ("shape", "chosen", "runner_up")}, indent=1))

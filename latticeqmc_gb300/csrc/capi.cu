@@ -294,7 +294,11 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
             const bool f32 = kind[c] == kTiledFp32, emu = kind[c] == kTiledFp64e;
             d.flags = 0;
             // the delayed-update buffers in shared memory when the target depth fits there,
-            // else in global memory; two tensor-core stage buffers unless they would cost depth
+            // else in global memory.  Tensor-core stage buffers (fp64e): the requested count,
+            // else three where they fit, else two, else one; a count that does not fit beside
+            // the delayed-update buffers moves them to global memory (same depth) -- at 16x16
+            // the deeper copy ring gains more (3 % of the sweep) than their shared-memory
+            // residence.
             const int target = lqmc::sweep_tiled_delay_target(f32, h->p.delay, emu);
             d.oz_stages = 1;
             d.delay = lqmc::sweep_tiled_delay(n, f32, h->p.delay, smem_cap, emu, 1);
@@ -303,22 +307,21 @@ int lqmc_set_chains(lqmc_handle* h, int32_t n_chains, const int32_t* n_sites,
                 xy_global = true;
                 d.delay = target;
                 d.flags |= lqmc::kUpdatesInGlobal;
-                if (emu && lqmc::sweep_tiled_smem_bytes(n, f32, d.delay, emu, 2, true) <= smem_cap) d.oz_stages = 2;
-            } else if (emu && lqmc::sweep_tiled_delay(n, f32, h->p.delay, smem_cap, emu, 2) >= d.delay) {
-                d.oz_stages = 2;
             }
-            // a requested stage count: fewer always fit; more may need the delayed-update
-            // buffers moved to global memory
-            const int want = h->p.oz_stages;
-            if (emu && want > 0 && want <= d.oz_stages) d.oz_stages = want;
-            if (emu && want > d.oz_stages) {
-                if (!xy_global && lqmc::sweep_tiled_smem_bytes(n, f32, d.delay, emu, want, false) > smem_cap) {
+            const int want = emu ? h->p.oz_stages : 0;
+            for (int st = emu ? (want > 0 ? want : kMaxOzStages) : 1; st > 1; --st) {
+                if (lqmc::sweep_tiled_smem_bytes(n, f32, d.delay, emu, st, xy_global) <= smem_cap) {
+                    d.oz_stages = st;
+                    break;
+                }
+                if (!xy_global && lqmc::sweep_tiled_smem_bytes(n, f32, target, emu, st, true) <= smem_cap) {
                     xy_global = true;
                     d.delay = target;
                     d.flags |= lqmc::kUpdatesInGlobal;
+                    d.oz_stages = st;
+                    break;
                 }
-                d.oz_stages = want;
-                if (lqmc::sweep_tiled_smem_bytes(n, f32, d.delay, emu, want, xy_global) > smem_cap) {
+                if (want > 0) {
                     release(h);
                     return fail(h, LQMC_ERR_UNSUPPORTED, "the requested stage buffers do not fit in shared memory");
                 }
