@@ -31,12 +31,12 @@ def test_second_pass_refines_around_the_fastest_passing_grid_point(monkeypatch, 
                         lambda specs, p, c, s, d=0, ref_cache=None: {
                             "max_dG": 1e-8, "chains_diverged": 0, "max_residual": 0.0,
                             "fp64_chains_flagged": 0,
-                            "chains_flagged": 0 if "udt" in c.get("fp64e_native", []) else 1})
+                            "chains_flagged": 0 if "lu" in c.get("fp64e_native", []) else 1})
     rec = at.autotune(16, 8.0, 80, "fp64e", cache=str(tmp_path / "t.json"), log=None)
     ch = rec["chosen"]
-    assert ch["stab_every"] == 8 and ch["delay"] == 32 and ch["fp64e_native"] == ["udt", "stack"]
+    assert ch["stab_every"] == 8 and ch["delay"] == 32 and ch["fp64e_native"] == ["lu", "lu_rhs"]
     kw = at.settings(rec)
-    assert kw["fp64e_native"] == ("udt", "stack") and kw["delay"] == 32
+    assert kw["fp64e_native"] == ("lu", "lu_rhs") and kw["delay"] == 32
 
 
 def test_fastest_setting_meeting_the_bar_is_chosen_and_cached(tmp_path, monkeypatch):

@@ -24,10 +24,10 @@ pytestmark = pytest.mark.gpu
 # "upward" way while sweeping down (lqmc.py:337-345) without stabilisation, so rounding
 # differences grow within a sweep and spike where an update is near-singular.  The largest
 # differences this kernel reaches over the recorded runs are 5.6e-6 (2x2, 40 sweeps),
-# 1.1e-5 (4x4) and 9.6e-7 (8x8); the floors are about ten times those.  (A numpy shadow of the
-# same math with another summation order has reached 4.6e-9, 1.1e-2 and 9.6e-5: the
-# amplification, not the kernel, sets the scale.)
-COMPAT_G_FLOOR = {2: 5e-5, 4: 1e-4, 8: 1e-5}
+# 7.6e-5 (4x4, 8 sweeps) and 1.7e-5 (8x8, 2 sweeps); the floors are about ten times those.
+# (A numpy shadow of the same math with another summation order has reached 4.6e-9, 1.1e-2
+# and 9.6e-5: the amplification, not the kernel, sets the scale.)
+COMPAT_G_FLOOR = {2: 5e-5, 4: 1e-3, 8: 2e-4}
 
 
 @pytest.mark.parametrize("side", [2, 4, 8])
