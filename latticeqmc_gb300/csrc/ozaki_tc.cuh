@@ -245,29 +245,47 @@ __device__ __noinline__ void split_tiles(const double* x, int ld, bool trans, in
                             __nv_bfloat16* dst, int* scratch, const int* kshift = nullptr) {
     const int kp = kpad(k), S = kp / kBK, rp = rows_pad(rows, BLK);
     if (!trans) {
-        // one warp per row: lanes read 8 consecutive k each (a warp covers 256 contiguous
-        // elements), then one warp max-reduction
+        // a warp takes rpw rows at a time, lpr lanes per row (lanes read 8 consecutive k each,
+        // lpr the fewest lanes that cover k, at most 32), and kRowSets such row sets at once:
+        // every load of a warp's rows is in flight together, one reduction per row set
+        constexpr int kRowSets = 4;
         const int lane = lane_id();
-        for (int r = warp_id(); r < rows; r += kNW) {
-            int emax = 0;
-            for (int q0 = 8 * lane; q0 < k; q0 += 256) {
+        const int lpr = k <= 8 ? 1 : k <= 16 ? 2 : k <= 32 ? 4 : k <= 64 ? 8 : k <= 128 ? 16 : 32;
+        const int rpw = 32 / lpr, sub = lane / lpr, ql = lane % lpr;
+        for (int r0 = warp_id() * rpw; r0 < rows; r0 += kNW * rpw * kRowSets) {
+            int em[kRowSets];
 #pragma unroll
-                for (int c = 0; c < 8; ++c)
-                    if (q0 + c < k)
-                        emax = max(emax, biased_exp(x[(size_t)r * ld + q0 + c], kshift ? kshift[q0 + c] : 0));
+            for (int t = 0; t < kRowSets; ++t) em[t] = 0;
+            for (int q0 = 8 * ql; q0 < k; q0 += 8 * lpr) {
+#pragma unroll
+                for (int t = 0; t < kRowSets; ++t) {
+                    const int r = r0 + t * kNW * rpw + sub;
+                    if (r < rows) {
+#pragma unroll
+                        for (int c = 0; c < 8; ++c)
+                            if (q0 + c < k)
+                                em[t] = max(em[t], biased_exp(x[(size_t)r * ld + q0 + c], kshift ? kshift[q0 + c] : 0));
+                    }
+                }
             }
-            emax = __reduce_max_sync(0xffffffffu, emax);
-            if (lane == 0) scratch[r] = emax;
+#pragma unroll
+            for (int t = 0; t < kRowSets; ++t) {
+                for (int o = lpr / 2; o > 0; o >>= 1) em[t] = max(em[t], __shfl_xor_sync(0xffffffffu, em[t], o));
+                const int r = r0 + t * kNW * rpw + sub;
+                if (ql == 0 && r < rows) scratch[r] = em[t];
+            }
         }
     } else {
         // thread (group of 8 consecutive rows, stripe of k) keeps 8 maxima in registers while
-        // it walks its stripe (a warp, 32 groups of one k, reads contiguous memory); the
-        // stripes' maxima are combined through shared memory
+        // it walks its stripe (a warp, 32 groups of one k, reads contiguous memory), four k of
+        // the stripe per step so that their loads are in flight together; the stripes'
+        // maxima are combined through shared memory
         int* part = scratch + kScratchStripes;
         const int g8 = (rows + 7) / 8, nq = max(1, kNT / g8);
         if (threadIdx.x < g8 * nq) {
             const int r0 = (threadIdx.x % g8) * 8, qs = threadIdx.x / g8;
             int em[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll 4
             for (int q = qs; q < k; q += nq) {
                 const int off = kshift ? kshift[q] : 0;
 #pragma unroll
