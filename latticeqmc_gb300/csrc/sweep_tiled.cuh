@@ -220,16 +220,36 @@ __device__ int householder_panel_cm(double* s, double* tau, int n, int jb, int b
         const double den = sv[kNW];
         for (int i = j + 1 + threadIdx.x; i < n; i += kNT) cj[i] = cj[i] / den;
         __syncthreads();
-        for (int k = j + 1 + warp_id(); k < jb + b; k += kNW) {
-            double* ck = s + (size_t)k * n;
-            double acc = 0.0;
-#pragma unroll 4
-            for (int i = j + 1 + lane; i < n; i += 32) acc = fma(cj[i], ck[i], acc);
-            acc = warp_sum(acc);
-            const double wk = t * (ck[j] + acc);
+        // a warp updates kCols later columns of the panel at once (their loads in flight
+        // together); per column the same operations in the same order as one at a time
+        constexpr int kCols = 4;
+        for (int k0 = j + 1 + warp_id() * kCols; k0 < jb + b; k0 += kNW * kCols) {
+            const int nc = min(kCols, jb + b - k0);
+            double acc[kCols];
+#pragma unroll
+            for (int c = 0; c < kCols; ++c) acc[c] = 0.0;
+#pragma unroll 2
+            for (int i = j + 1 + lane; i < n; i += 32) {
+                const double v = cj[i];
+#pragma unroll
+                for (int c = 0; c < kCols; ++c)
+                    if (c < nc) acc[c] = fma(v, s[(size_t)(k0 + c) * n + i], acc[c]);
+            }
+            double wk[kCols];
+#pragma unroll
+            for (int c = 0; c < kCols; ++c) {
+                acc[c] = warp_sum(acc[c]);
+                wk[c] = (c < nc) ? t * (s[(size_t)(k0 + c) * n + j] + acc[c]) : 0.0;
+            }
             for (int i = j + lane; i < n; i += 32) {
                 const double vi = (i == j) ? 1.0 : cj[i];
-                ck[i] = fma(-vi, wk, ck[i]);
+#pragma unroll
+                for (int c = 0; c < kCols; ++c) {
+                    if (c < nc) {
+                        double* ck = s + (size_t)(k0 + c) * n;
+                        ck[i] = fma(-vi, wk[c], ck[i]);
+                    }
+                }
             }
         }
         __syncthreads();
