@@ -274,9 +274,8 @@ int lqmc_abi_version(void);
  * writes every scratch value before reading it, so nothing needs clearing): calls that
  * overlap on the GPU -- on different streams, or from different host threads -- race and
  * must be serialised by the caller.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) for that device; make that first call before any
- * stream capture.  Asynchronous on `stream` (NULL = default stream); results are valid
- * once the stream has been synchronised.
+ * device address (cudaGetSymbolAddress) for that device.  Asynchronous on `stream` (NULL =
+ * default stream); results are valid once the stream has been synchronised.
  * --------------------------------------------------------------------------------------- */
 #define LQMC_STATIC_SCRATCH_BYTES (4u << 20)
 #define LQMC_STATIC_MAX_SITES 64

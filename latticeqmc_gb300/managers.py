@@ -100,6 +100,10 @@ class SerialProcessManager(_Manager):
         self.result = np.swapaxes(np.array([gf_up, gf_dn]), 0, 1)
 
     def delete_cache(self):
+        """Remove ``tmp_gf_series.npz`` from the working directory: the resume cache that
+        measure_betas writes while it runs with caching=True (the reference's manager keeps its
+        cache under the same name, lqmc/multiprocessing.py:313-333, so one left by an
+        interrupted reference run in the same directory is removed too)."""
         if os.path.isfile(self._tmp_file):
             os.remove(self._tmp_file)
 
