@@ -86,3 +86,31 @@ def test_status_counts_every_bit():
     c = bench.status_counts(np.array([0, 1, 2, 4, 8, 12]))
     assert c == {"chains_nonfinite": 1, "chains_singular": 1, "chains_drift": 2,
                  "chains_timeout": 2, "chains_flagged": 5}
+
+
+def test_tuned_settings_take_the_fastest_passing_candidate_in_the_workloads_range(monkeypatch):
+    """bench.tuned_settings: candidates outside the workload's stab_every range are skipped,
+    every tuned setting (native categories included) reaches the engine, and the record's
+    chosen and runner-up are reported."""
+    import argparse
+    from latticeqmc_gb300 import autotune
+
+    def row(stab, sec, ok, **kw):
+        return dict({"stab_every": stab, "delay": 0, "sweep_order": "alternate", "oz_stages": 0,
+                     "fp64e_native": [], "seconds_per_sweep": sec, "ok": ok, "max_dG": 1e-9,
+                     "chains_flagged": 0 if ok else 1, "max_residual": 1e-7}, **kw)
+    rec = {"chains": 64, "tol": 1e-6, "chosen": None,
+           "candidates": [row(4, 0.30, True), row(6, 0.47, True, delay=48),
+                          row(6, 0.48, True, fp64e_native=["lu"]), row(8, 0.42, False),
+                          row(20, 0.35, True)]}
+    monkeypatch.setattr(autotune, "tuned", lambda *a: rec)
+    args = argparse.Namespace(workload="square16_beta8")
+    cfg = {"sides": [16], "beta": 8.0, "L": 80, "stab_every": 8}
+    kw, info = bench.tuned_settings(args, cfg, "fp64e")
+    assert kw == {"stab_every": 6, "delay": 48, "sweep_order": "alternate", "fp64e_native": ()}
+    assert info["chosen"]["seconds_per_sweep"] == 0.47
+    assert info["runner_up"]["fp64e_native"] == ["lu"]
+    assert info["candidates_passing"] == 4
+    monkeypatch.setattr(autotune, "tuned", lambda *a: None)
+    kw, info = bench.tuned_settings(args, cfg, "fp64e")
+    assert kw == {"stab_every": 8, "sweep_order": "alternate"} and "defaults" in info["source"]
