@@ -66,8 +66,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "site-updates/s (sweeps/s beside it), DQMC sweep of batched Markov chains"
 UNIT = "site-updates/s"
-# DRAM traffic of one fp64e sweep launch of the square16_beta8 workload (64 chains), from ncu
-FP64E_TRAFFIC = 4.106e11
+# DRAM traffic of one fp64e sweep launch of the square16_beta8 workload (64 chains, the tuned
+# settings), from ncu: dram__bytes_read.sum + dram__bytes_write.sum, mean of 2 launches
+FP64E_TRAFFIC = 2.774e11
 STATUS_BITS = {"nonfinite": 1, "singular": 2, "drift": 4, "timeout": 8}
 
 
