@@ -100,7 +100,7 @@ struct TSmem {
     double* ev;
     double* nrm;
     double* tau;
-    double* dv;
+    double* dv;       // site updates: the running diagonal of X Y^T (udt: the new d)
     int* order;
     double* sv;
     T* ev_t;      // exp_v of the current slice in precision T
@@ -877,6 +877,7 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int step
     int* fv = sm.order;        // [n] the slice's field values at its start
     T* cnext = sm.xt[1];       // [n] G[:, i + 1]
     T* rnext = sm.yt[1];       // [n] G[i + 1, :]
+    double* dsum = sm.dv;      // [n] (X Y^T)_jj of the pending updates, kept by row j's thread
     {
         const size_t base = (size_t)step * n;
         if (d.rng == LQMC_RNG_REPLAY) {
@@ -896,6 +897,7 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int step
         for (int i = threadIdx.x; i < n; i += kNT) {
             fv[i] = f[i];
             gdiag[i] = (double)g[(size_t)i * n + i];
+            dsum[i] = 0.0;
         }
         __syncthreads();
     }
@@ -911,24 +913,18 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int step
     for (int i = 0; i < n; ++i) {
         const int s_il = fv[i];
         const int par = 2 * (i & 1);
-        if (warp_id() == 0) {
+        if (threadIdx.x == 0) {
             // this spin's factor R_sigma = 1 + D_sigma (1 - G_eff,ii) and its update
-            // coefficient D_sigma / R_sigma, once per CTA; the factors are exchanged
-            const int lane = lane_id();
-            T part = T(0);
-            for (int q = lane; q < m; q += 32) part = fma(sm.dx[(size_t)i * ld + q], sm.dy[(size_t)i * ld + q], part);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-            if (lane == 0) {
-                const double gv = (double)((T)gdiag[i] - part);
-                const double ep = s_il > 0 ? d.c[0] : d.c[1];
-                const double em = s_il > 0 ? d.c[1] : d.c[0];
-                const double dl = (sp ? em : ep) - 1.0;
-                const double r = 1.0 + dl * (1.0 - gv);
-                sm.gii[par + sp] = r;
-                sm.peer_gii[par + sp] = r;
-                sm.gii[4 + (i & 1)] = dl / r;
-            }
+            // coefficient D_sigma / R_sigma, once per CTA; the factors are exchanged.
+            // G_eff,ii = G_ii - (X Y^T)_ii, the latter kept up to date by row i's thread
+            const double gv = (double)((T)gdiag[i] - (T)dsum[i]);
+            const double ep = s_il > 0 ? d.c[0] : d.c[1];
+            const double em = s_il > 0 ? d.c[1] : d.c[0];
+            const double dl = (sp ? em : ep) - 1.0;
+            const double r = 1.0 + dl * (1.0 - gv);
+            sm.gii[par + sp] = r;
+            sm.peer_gii[par + sp] = r;
+            sm.gii[4 + (i & 1)] = dl / r;
         }
         // the next site's row and column are in flight while this one is decided (each thread
         // copies and later reads only its own rows j)
@@ -961,8 +957,10 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int step
                     cu = fma(-sm.dx[(size_t)j * ld + p], sm.dy[(size_t)i * ld + p], cu);   // G_eff[j][i]
                     rv = fma(-sm.dx[(size_t)i * ld + p], sm.dy[(size_t)j * ld + p], rv);   // G_eff[i][j]
                 }
+                const T yn = ((j == i ? T(1) : T(0)) - rv) * a;
                 sm.dx[(size_t)j * ld + m] = cu;
-                sm.dy[(size_t)j * ld + m] = ((j == i ? T(1) : T(0)) - rv) * a;
+                sm.dy[(size_t)j * ld + m] = yn;
+                dsum[j] = fma((double)cu, (double)yn, dsum[j]);
             }
             if (threadIdx.x == 0) {
                 f[i] = (int8_t)(-s_il);   // both CTAs write the same value
@@ -979,7 +977,10 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int step
                 if (threadIdx.x == 0) sm.sub[6] += clock64() - tf;
                 m = 0;
                 flushed = true;
-                for (int j = threadIdx.x; j < n; j += kNT) gdiag[j] = (double)g[(size_t)j * n + j];
+                for (int j = threadIdx.x; j < n; j += kNT) {
+                    gdiag[j] = (double)g[(size_t)j * n + j];
+                    dsum[j] = 0.0;
+                }
                 __syncthreads();
             }
         }
