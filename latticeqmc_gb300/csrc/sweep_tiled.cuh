@@ -953,6 +953,9 @@ __device__ void update_slice_t(const ChainDesc& d, TSmem<T>& sm, int l, int step
                 const int j = threadIdx.x + q * kNT;
                 if (j >= n) break;
                 T cu = colv[q], rv = rowv[q];
+                // unrolled so that the loads of several p (X and Y may live in global memory)
+                // are in flight together; the FMA order per output is unchanged
+#pragma unroll 4
                 for (int p = 0; p < m; ++p) {
                     cu = fma(-sm.dx[(size_t)j * ld + p], sm.dy[(size_t)i * ld + p], cu);   // G_eff[j][i]
                     rv = fma(-sm.dx[(size_t)i * ld + p], sm.dy[(size_t)j * ld + p], rv);   // G_eff[i][j]
