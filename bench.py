@@ -10,14 +10,18 @@ the time per sweep; sweeps/s is reported beside it.  Inputs are synthetic random
 
 Workload square16_beta8 (default; the configuration the metric "batched mixed vs plain
 FP64 at max|dG| <= 1e-6" is quoted on): 64 chains of 16x16 (N=256), U=4, beta=8, dtau=0.1
-(L=80), dqmc, stabilisation every 8 slices, on-device Philox uniforms.  `value` is the
-batched mixed-precision engine that meets the max|dG| <= 1e-6 bar: precision "fp64e", every
-dense product (wraps, B-chain, delayed rank-k updates, the blocked QR's updates) a
-float64-accurate GEMM emulated on the tcgen05 BF16 tensor cores, the per-site updates,
-panel factorisations and the LU in float64.  `fp64` carries the plain float64 engine on
-the same workload (throughput and the speed-up of `value` over it) and `fp32_mixed` the
-float32 engine; `accuracy` compares fp64e with fp64 over several sweeps from identical
-fields and uniforms.  Time-bounded sub-records of the other workloads ride on the same line:
+(L=80), dqmc, on-device Philox uniforms; stabilisation interval, sweep order, delay depth,
+stage count and native-float64 categories of the headline engine from the project
+autotuner's record for this shape (latticeqmc_gb300/tuning/autotune.json; stab_every within
+6-16, see STAB_RANGE), else stabilisation every 8 slices in the alternating order.  `value`
+is the batched mixed-precision engine that meets the max|dG| <= 1e-6 bar: precision "fp64e",
+every dense product (wraps, B-chain, delayed rank-k updates, the blocked QR's and the LU's
+updates) a float64-accurate GEMM emulated on the tcgen05 BF16 tensor cores, the per-site
+updates and the panel factorisations in float64.  `fp64` carries the plain float64 engine
+on the same workload, stabilisation interval and sweep order (throughput and the speed-up of
+`value` over it) and `fp32_mixed` the float32 engine; `accuracy` compares fp64e with fp64
+over several sweeps from identical fields and uniforms; `tuning` names the chosen setting
+and the runner-up.  Time-bounded sub-records of the other workloads ride on the same line:
 `batched_fp64` (512 uneven chains against the same chains run one at a time) and
 `square32_beta6` (32x32 chains, fp64e).
 
