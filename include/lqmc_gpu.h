@@ -108,7 +108,8 @@ typedef struct lqmc_params {
     int32_t precision;     /* LQMC_PREC_*                                                  */
     int32_t rng;           /* LQMC_RNG_*                                                   */
     int32_t stab_every;    /* slices between from-scratch refreshes (dqmc); 0 -> 10        */
-    int32_t delay;         /* delayed-update depth k for LQMC_PREC_MIXED; 0 -> automatic   */
+    int32_t delay;         /* delayed-update depth k of the tiled kernel; 0 -> 24 fp64e, 16
+                              fp64, 32 mixed (X, Y move to global memory rather than shrink k) */
     int32_t record;        /* 1: keep per-site accept decisions of the last lqmc_sweep    */
     uint64_t seed;         /* Philox key word 0 (LQMC_RNG_PHILOX)                          */
     int32_t device;        /* CUDA device ordinal                                          */
